@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Gate-sweep benchmark of the GB300 state-vector engine.
+
+Workload: the 30-qubit layered random circuit family — per layer a
+Haar-random 1-qubit unitary on every qubit, then CNOTs on a random perfect
+matching (15 CNOTs) — on a complex128 state (16 GiB, far larger than the
+129 MB L2, so no flush is needed between steps). One step = one layer
+(45 gates), applied through the reference-facing call (qs_try_apply_fast, one
+call per gate, matrices from host memory). Synthetic seeded gates (SplitMix64).
+
+metric: HBM GB/s per gate sweep = sum over gates of the algorithmic bytes
+(one read + one write of every amplitude a gate changes: 2*N*16 for a dense
+1-qubit gate, N*16 for a CNOT) / time.
+
+`--impl reference` times the reference algorithm on the host (the C
+restatement of Register::try_apply_fast in oracle/, single-threaded like the
+reference) on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30-qubit gate-sweep HBM GB/s"
+UNIT = "GB/s"
+FALLBACK_HBM_GBS = 6800.0
+FP64_PEAK_TFLOPS_MEASURED = 1.194  # FP64 FMA rate measured on this machine's GB300 (8 independent chains/thread)
+
+
+def gate_bytes(op, n: int, amp_bytes: int) -> float:
+    """Algorithmic HBM bytes of one gate sweep (read + write of each amplitude the gate changes)."""
+    m = np.asarray(op.matrix)
+    N = float(1 << n)
+    k = len(op.targets)
+    if k == 1 and not (m[0, 1] == 0 and m[1, 0] == 0 and m[0, 0] == 1):  # dense or anti-diagonal 1q
+        return 2.0 * N * amp_bytes
+    if k == 2 and np.array_equal(m, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]])):
+        return 2.0 * (N / 2) * amp_bytes  # CNOT: the control = 1 half
+    return 2.0 * N * amp_bytes
+
+
+def is_haar(op) -> bool:
+    return len(op.targets) == 1
+
+
+def read_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def read_traffic() -> float | None:
+    p = ROOT / "profiles" / "roofline_traffic.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dense1_c128_30q_bytes_per_launch"])
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU (reference algorithm) timing
+def cpu_reference_gbps(n: int, layers, budget_s: float, max_gates: int | None = None) -> dict:
+    """Time the oracle's restatement of Register::try_apply_fast, one gate after another, for about budget_s."""
+    from oracle.oracle import OracleRegister
+
+    reg = OracleRegister.from_int(n, 0)
+    gates = [g for layer in layers for g in layer]
+    done, nbytes = 0, 0.0
+    t0 = time.perf_counter()
+    for g in gates:
+        reg.try_apply_fast(g.matrix, g.targets)
+        done += 1
+        nbytes += gate_bytes(g, n, 16)
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_gates and done >= max_gates):
+            break
+    el = time.perf_counter() - t0
+    return {"gbps": nbytes / el / 1e9, "gates": done, "seconds": el, "gates_per_s": done / el}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from quaru_gb300.workloads import layered_circuit, seed_for
+
+    n = args.ref_qubits
+    layers = layered_circuit(n, 2, seed_for(3))
+    gates = [g for layer in layers for g in layer]
+    from oracle.oracle import OracleRegister
+
+    reg = OracleRegister.from_int(n, 0)
+    per_step = []
+    total_bytes = 0.0
+    total_t = 0.0
+    gi = 0
+    for step in range(args.warmup + args.steps):
+        g = gates[gi % len(gates)]
+        gi += 1
+        t0 = time.perf_counter()
+        reg.try_apply_fast(g.matrix, g.targets)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            per_step.append(dt)
+            total_bytes += gate_bytes(g, n, 16)
+            total_t += dt
+    value = total_bytes / total_t / 1e9
+    sample = (f"{n}-qubit instance of the layered family, one gate per step (Haar 1q or CNOT), "
+              f"oracle/ C restatement of Register::try_apply_fast (clone + per-tuple gather/mat-vec/scatter)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"layered random circuit, {n} qubits (host), complex128", "qubits": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    import quaru_gb300 as q
+    from quaru_gb300 import _lib
+    from quaru_gb300.workloads import layered_circuit, seed_for
+
+    lib = _lib.load()
+    n = args.qubits
+    arith = {"exact": q.QS_ARITH_EXACT, "fma": q.QS_ARITH_FMA, "df64": q.QS_ARITH_DF64}[args.arith]
+    prec = q.QS_PREC_C64 if args.precision == "c64" else q.QS_PREC_C128
+    amp = 8 if prec == q.QS_PREC_C64 else 16
+    nlayers = max(args.warmup + args.steps, 1)
+    layers = layered_circuit(n, min(nlayers, 40), seed_for(3))
+    reg = q.Register.from_int(n, 0, precision=prec)
+    reg.set_arith(arith)
+    stream = torch.cuda.ExternalStream(reg.stream)
+
+    def layer(i):
+        return layers[i % len(layers)]
+
+    def barrier():
+        reg.synchronize()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # ---- device-timed loop: inputs resident, no host read-back
+    for i in range(args.warmup):
+        for g in layer(i):
+            reg.try_apply_fast(g)
+    barrier()
+    haar_events = []
+    step_bytes = 0.0
+    launches0 = lib.qs_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for i in range(args.warmup, args.warmup + args.steps):
+            for g in layer(i):
+                if is_haar(g) and len(haar_events) < 64:
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    reg.try_apply_fast(g)
+                    b.record(stream)
+                    haar_events.append((a, b))
+                else:
+                    reg.try_apply_fast(g)
+                step_bytes += gate_bytes(g, n, amp)
+        ev1.record(stream)
+        barrier()
+        launches = lib.qs_launch_count() - launches0
+        dev_s = ev0.elapsed_time(ev1) / 1e3
+
+        # ---- end-to-end loop: host gate data in, a host read-back of a result every step
+        for i in range(args.warmup):
+            for g in layer(i):
+                reg.try_apply_fast(g)
+            reg_p = reg  # noqa: F841
+        barrier()
+        h2d = 0
+        t0 = time.perf_counter()
+        for i in range(args.warmup, args.warmup + args.steps):
+            for g in layer(i):
+                reg.try_apply_fast(g)
+                h2d += np.asarray(g.matrix).nbytes + 8 * len(g.targets)
+            p0 = _measure_probs(lib, reg, 0)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+    clk = clocks.summary()
+
+    t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_s, e2e_s = float(t[0]), float(t[1])
+    total_bytes = step_bytes * world
+    value = total_bytes / dev_s / 1e9
+    e2e = total_bytes / e2e_s / 1e9
+
+    haar_ms = [a.elapsed_time(b) for a, b in haar_events]
+    avg_haar_s = statistics.mean(haar_ms) / 1e3 if haar_ms else float("nan")
+    per_launch_bytes = 2.0 * (1 << n) * amp
+    achieved = per_launch_bytes / avg_haar_s / 1e9
+    peak, peak_kind = read_peaks()
+    flops_per_launch = (1 << n) * 8 * 2.0  # 8 FMAs per amplitude for a dense complex 2x2
+    gates_per_step = len(layer(0))
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        r = cpu_reference_gbps(args.cpu_qubits, layered_circuit(args.cpu_qubits, 2, seed_for(3)), args.cpu_budget)
+        cpu = {"value": r["gbps"], "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_qubits}-qubit instance of the layered family, first {r['gates']} gates "
+                         f"({r['seconds']:.1f} s), oracle/ C restatement of Register::try_apply_fast, 1 thread "
+                         f"(the reference is single-threaded)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == q.QS_PREC_C64 else "f64",
+        "data": "synthetic (seeded Haar 1q + CNOT matchings, SplitMix64)",
+        "config": {"workload": f"{n}-qubit layered random circuit (per layer: Haar 1q on all {n} qubits + "
+                               f"{n // 2} CNOTs on a random perfect matching), one layer per step",
+                   "qubits": n, "precision": args.precision, "arith": args.arith, "fuse": 0,
+                   "gates_per_step": gates_per_step, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": f"state {(1 << n) * amp / 2**30:.0f} GiB >> 129 MB L2: inputs larger than L2, no flush"},
+        "gates_per_s": gates_per_step * args.steps * world / dev_s,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": 16},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "k_dense1 (dense 1-qubit gate sweep)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": read_traffic(),
+                     "peak_source": peak_kind,
+                     "fp64_pipe": {"achieved_tflops": flops_per_launch / avg_haar_s / 1e12,
+                                   "peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
+                                   "frac": flops_per_launch / avg_haar_s / 1e12 / FP64_PEAK_TFLOPS_MEASURED}},
+        "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "probe": {"p0_qubit0": p0},
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def _measure_probs(lib, reg, target: int) -> float:
+    import ctypes
+
+    p0, p1 = ctypes.c_double(0), ctypes.c_double(0)
+    rc = lib.qs_measure_probabilities(reg.handle, target, ctypes.byref(p0), ctypes.byref(p1), None)
+    if rc:
+        raise RuntimeError(f"qs_measure_probabilities failed: {rc}")
+    return p0.value
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
+    ap.add_argument("--arith", choices=["exact", "fma", "df64"], default="fma")
+    ap.add_argument("--cpu-qubits", type=int, default=24)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--ref-qubits", type=int, default=26)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps are required")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * quaru_gpu.h — C ABI of the GB300 state-vector engine (libquaru_gb300.so).
+ *
+ * Drop-in for the gate-application and measurement path of Quaru
+ * (DATX11-22/quaru). Each entry point names the reference item it replaces
+ * (path:line within the reference project). Plain pointers and sizes only:
+ * complex data is interleaved (re, im) IEEE doubles — the memory layout of
+ * ndarray's Array2<Complex<f64>> — and matrices are row-major 2^k x 2^k with
+ * local index bit j <-> targets[j] (src/register.rs:163-176).
+ *
+ * Threading: one register is used by one host thread at a time (Rust's
+ * `&mut self`); distinct registers may be used from distinct threads. Every
+ * call is ordered on the register's own CUDA stream; calls that return data
+ * to the host synchronise that stream. No exception crosses this boundary.
+ *
+ * Return value: QS_OK or a status below. `err` (nullable, 3 entries) carries
+ * the payload of OperationError (src/register.rs:10-20): InvalidTarget(t) ->
+ * err[0] = t; InvalidDimensions(r, c) -> err[0] = r, err[1] = c;
+ * InvalidArity(k) -> err[0] = k; InvalidQubit(i) -> err[0] = i. Circuit calls
+ * put the failing gate's index in err[2]. qs_last_error() gives a message.
+ */
+#ifndef QUARU_GPU_H
+#define QUARU_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define QS_OK 0
+#define QS_INVALID_TARGET 1     /* OperationError::InvalidTarget */
+#define QS_INVALID_DIMENSIONS 2 /* OperationError::InvalidDimensions */
+#define QS_INVALID_ARITY 3      /* OperationError::InvalidArity */
+#define QS_INVALID_QUBIT 4      /* OperationError::InvalidQubit */
+#define QS_INVALID_ARGUMENT 5   /* null pointer, n out of range, bad enum */
+#define QS_CUDA_ERROR 6         /* a CUDA runtime call failed */
+#define QS_OUT_OF_MEMORY 7      /* device allocation failed */
+#define QS_TIMEOUT 8            /* a bounded device wait gave up */
+
+/* ---- state precision ---------------------------------------------------- */
+#define QS_PREC_C128 0 /* complex128 state (the reference's c64 = Complex<f64>) */
+#define QS_PREC_C64 1  /* complex64 state: the mixed-precision form */
+
+/* ---- arithmetic of gate application on a complex128 register ------------ */
+#define QS_ARITH_EXACT 0 /* the reference's operation order, no fused multiply-add:
+                            bit-identical amplitudes (+0 and -0 compared as equal) */
+#define QS_ARITH_FMA 1   /* FP64 fused multiply-add; within 1e-15 relative per gate */
+#define QS_ARITH_DF64 2  /* double-float arithmetic on the FP32 pipe for dense gates;
+                            ~2^-47 relative per gate; permutation/diagonal gates stay exact */
+
+typedef struct qs_register qs_register;
+
+/* ---- construction / lifetime -------------------------------------------- */
+
+/* Register::new (src/register.rs:41-56): basis state from n booleans. */
+int qs_register_new(const uint8_t* bits, size_t n, int precision, qs_register** out);
+
+/* Register::from_int (src/register.rs:58-63): basis state |k> on n qubits. */
+int qs_register_from_int(size_t n, size_t k, int precision, qs_register** out);
+
+/* Register::try_from_qubits (src/register.rs:81-102): product state from n
+ * single-qubit states (2 complex each, 4 doubles). InvalidQubit(i) when
+ * |sum |q_i|^2 - 1| >= 1e-6 (src/register.rs:107-115). */
+int qs_register_try_from_qubits(const double* qubits, size_t n, int precision,
+                                qs_register** out, size_t* err);
+
+/* #[derive(Clone)] on Register (src/register.rs:23): device-to-device copy. */
+int qs_register_clone(const qs_register* src, qs_register** out);
+
+/* Drop for Register. Null is ignored. */
+void qs_register_free(qs_register* reg);
+
+/* Register::size (src/register.rs:404-406). */
+size_t qs_register_size(const qs_register* reg);
+
+/* Precision the register was created with (QS_PREC_*). */
+int qs_register_precision(const qs_register* reg);
+
+/* Select the arithmetic of later gate applications (QS_ARITH_*); default
+ * QS_ARITH_EXACT. Ignored by complex64 registers (FP32 FMA). */
+int qs_register_set_arith(qs_register* reg, int arith);
+
+/* ---- gate application --------------------------------------------------- */
+
+/* Register::try_apply_fast (src/register.rs:140-191); Register::apply
+ * (:134-137) is this call plus a panic on error. Validation order: shape
+ * (InvalidDimensions), duplicate target (smallest duplicate), out-of-range
+ * target (first in list order). The shape check rejects every shape that is
+ * not 2^k x 2^k; the reference's own check (:141-145) fires only on (k, k)
+ * and otherwise panics inside ndarray's dot, so every call the reference
+ * rejects is rejected here with the same payload. */
+int qs_try_apply_fast(qs_register* reg, const double* matrix, size_t rows, size_t cols,
+                      const size_t* targets, size_t k, size_t* err);
+
+/* Register::try_apply_all (src/register.rs:267-281): a 1-qubit operation on
+ * every qubit, as n in-place sweeps instead of a dense 2^n x 2^n kron.
+ * InvalidArity(k) when k != 1. */
+int qs_try_apply_all(qs_register* reg, const double* matrix, size_t rows, size_t cols,
+                     size_t k, size_t* err);
+
+/* One gate of a circuit: arity k, k targets, 2^k x 2^k interleaved matrix. */
+typedef struct qs_gate {
+    size_t k;
+    const size_t* targets;
+    const double* matrix;
+} qs_gate;
+
+/* Options for qs_apply_circuit. */
+typedef struct qs_circuit_options {
+    int fuse;        /* 0: one sweep per gate; 1: cache-blocked stages (bit-identical to 0
+                        under QS_ARITH_EXACT); 2: dense fused blocks (complex64 registers:
+                        3xTF32 tensor-core blocks) */
+    int max_width;   /* widest fused dense block, 2..5 (fuse == 2) */
+    int tile_qubits; /* qubits per shared-memory tile for fuse >= 1; 0 = automatic */
+    int reserved;
+} qs_circuit_options;
+
+/* The operations loop of Register::apply_circuit (src/register.rs:345-350):
+ * applies gates[0..m) in order. Every gate is validated before any is
+ * applied; on error nothing is applied, err[2] = index of the bad gate.
+ * opts may be null (fuse = 0). */
+int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m,
+                     const qs_circuit_options* opts, size_t* err);
+
+/* ---- measurement -------------------------------------------------------- */
+
+/* Register::try_measure (src/register.rs:297-342) with the uniform draw in
+ * [0, 1) supplied by the caller (the reference's thread_rng, :317-318, cannot
+ * be seeded). outcome = draw > prob_0 (:321). prob0/prob1 are nullable and
+ * receive the FP64 probability sums before the collapse. */
+int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
+                   double* prob0, double* prob1, size_t* err);
+
+/* The probability sums of try_measure (src/register.rs:303-315) without the
+ * draw and the collapse: p0 = sum |a_i|^2 over target bit 0, p1 over bit 1,
+ * FP64 on the GPU. The state is left unchanged. */
+int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, double* prob1, size_t* err);
+
+/* ---- host views ---------------------------------------------------------- */
+
+/* Read `pub state` (src/register.rs:35): 2^n complex, interleaved doubles. */
+int qs_get_state(const qs_register* reg, double* dst);
+
+/* Assign `pub state` (as examples/quantum_teleportation.rs:55-58 does). */
+int qs_set_state(qs_register* reg, const double* src);
+
+/* norm_sqr per amplitude, the numbers print_probabilities prints
+ * (src/register.rs:379-384), computed on the GPU in FP64. */
+int qs_probabilities(const qs_register* reg, double* dst);
+
+/* PartialEq for Register (src/register.rs:409-413): equal when every
+ * |a_i - b_i| < tol (the reference uses 1e-8). */
+int qs_register_eq(const qs_register* a, const qs_register* b, double tol, int* equal);
+
+/* Wait for all work queued on the register. */
+int qs_synchronize(qs_register* reg);
+
+/* The register's CUDA stream (cudaStream_t), for callers that time or order work. */
+void* qs_register_stream(qs_register* reg);
+
+/* Message for the last error on the calling host thread. */
+const char* qs_last_error(void);
+
+/* Number of kernels this library has launched in the process (all registers).
+ * Diagnostic without a counterpart in the reference. */
+uint64_t qs_launch_count(void);
+
+/* Library version string. */
+const char* qs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUARU_GPU_H */

@@ -1,0 +1,374 @@
+// qs_api.cu — the extern "C" boundary (include/quaru_gpu.h).
+//
+// Each function mirrors one item of Quaru's Register API (src/register.rs),
+// with OperationError mapped to status codes and a thread-local message. A
+// register owns one device buffer, one CUDA stream and small scratch areas.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "qs_circuit.h"
+#include "qs_internal.h"
+#include "qs_kernels.h"
+
+struct qs_register {
+    int n = 0;
+    int prec = QS_PREC_C128;
+    int arith = QS_ARITH_EXACT;
+    int device = 0;
+    int sms = 1;
+    void* state = nullptr;
+    cudaStream_t stream = nullptr;
+    double* partials = nullptr;  // device: per-block reduction partials
+    double* dres = nullptr;      // device: small results
+    double* hres = nullptr;      // pinned host mirror of dres
+};
+
+namespace qs {
+static std::atomic<uint64_t> g_launches{0};
+void note_launches(uint64_t count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+}  // namespace qs
+
+namespace {
+
+constexpr int kMaxPartials = 4096;
+constexpr size_t kMaxQubits = 36;
+thread_local std::string g_last_error;
+
+int set_err(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return set_err(QS_OUT_OF_MEMORY, std::string(what) + ": out of device memory");
+    }
+    return set_err(QS_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define QS_CUDA(call, what)                             \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+size_t amp_bytes(int prec) { return prec == QS_PREC_C64 ? 8 : 16; }
+
+void destroy(qs_register* r) {
+    if (!r) return;
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->state) cudaFree(r->state);
+    if (r->partials) cudaFree(r->partials);
+    if (r->dres) cudaFree(r->dres);
+    if (r->hres) cudaFreeHost(r->hres);
+    if (r->stream) cudaStreamDestroy(r->stream);
+    delete r;
+}
+
+// Allocate a register with uninitialised state.
+int allocate(size_t n, int prec, qs_register** out) {
+    if (!out) return set_err(QS_INVALID_ARGUMENT, "output pointer is null");
+    *out = nullptr;
+    if (prec != QS_PREC_C128 && prec != QS_PREC_C64) return set_err(QS_INVALID_ARGUMENT, "unknown precision");
+    if (n > kMaxQubits) return set_err(QS_INVALID_ARGUMENT, "too many qubits for one GPU");
+    auto* r = new qs_register();
+    r->n = int(n);
+    r->prec = prec;
+    cudaError_t e = cudaGetDevice(&r->device);
+    if (e != cudaSuccess) {
+        delete r;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, r->device);
+    if (r->sms < 1) r->sms = 1;
+    const size_t bytes = (size_t(1) << n) * amp_bytes(prec);
+    if ((e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc(&r->state, bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&r->partials, 2 * kMaxPartials * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&r->dres, 64 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMallocHost(&r->hres, 64 * sizeof(double))) != cudaSuccess) {
+        destroy(r);
+        return cuda_fail(e, "allocating register");
+    }
+    *out = r;
+    return QS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* qs_last_error(void) { return g_last_error.c_str(); }
+const char* qs_version(void) { return "quaru-gb300 0.1 (sm_103a)"; }
+
+int qs_register_from_int(size_t n, size_t k, int precision, qs_register** out) {
+    if (n < 64 && k >= (size_t(1) << n)) return set_err(QS_INVALID_ARGUMENT, "basis index out of range");
+    int rc = allocate(n, precision, out);
+    if (rc) return rc;
+    cudaError_t e = qs::launch_init_basis((*out)->state, int(n), precision, k, (*out)->stream, (*out)->sms);
+    if (e != cudaSuccess) {
+        destroy(*out);
+        *out = nullptr;
+        return cuda_fail(e, "init_basis");
+    }
+    return QS_OK;
+}
+
+int qs_register_new(const uint8_t* bits, size_t n, int precision, qs_register** out) {
+    if (n > 0 && !bits) return set_err(QS_INVALID_ARGUMENT, "bits is null");
+    if (n > kMaxQubits) return set_err(QS_INVALID_ARGUMENT, "too many qubits for one GPU");
+    // kron of |0>/|1> vectors (src/register.rs:47-50) is the basis state sum(bits[i] << i).
+    size_t k = 0;
+    for (size_t i = 0; i < n; i++)
+        if (bits[i]) k |= size_t(1) << i;
+    return qs_register_from_int(n, k, precision, out);
+}
+
+int qs_register_try_from_qubits(const double* qubits, size_t n, int precision, qs_register** out,
+                                size_t* err) {
+    if (!out) return set_err(QS_INVALID_ARGUMENT, "output pointer is null");
+    *out = nullptr;
+    if (n > 0 && !qubits) return set_err(QS_INVALID_ARGUMENT, "qubits is null");
+    if (n > 64) return set_err(QS_INVALID_ARGUMENT, "too many qubits for one GPU");
+    for (size_t q = 0; q < n; q++) {  // is_one (src/register.rs:107-115)
+        double total = -1.0;
+        for (int j = 0; j < 2; j++) {
+            const double re = qubits[4 * q + 2 * j], im = qubits[4 * q + 2 * j + 1];
+            total += re * re + im * im;
+        }
+        if (!(std::fabs(total) < 0.000001)) {
+            if (err) err[0] = q;
+            return set_err(QS_INVALID_QUBIT, "InvalidQubit(" + std::to_string(q) + ")");
+        }
+    }
+    int rc = allocate(n, precision, out);
+    if (rc) return rc;
+    cudaError_t e = qs::launch_init_product((*out)->state, int(n), precision, qubits, (*out)->stream, (*out)->sms);
+    if (e != cudaSuccess) {
+        destroy(*out);
+        *out = nullptr;
+        return cuda_fail(e, "init_product");
+    }
+    return QS_OK;
+}
+
+int qs_register_clone(const qs_register* src, qs_register** out) {
+    if (!src) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    int rc = allocate(size_t(src->n), src->prec, out);
+    if (rc) return rc;
+    (*out)->arith = src->arith;
+    cudaError_t e = cudaStreamSynchronize(src->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync((*out)->state, src->state, (size_t(1) << src->n) * amp_bytes(src->prec),
+                            cudaMemcpyDeviceToDevice, (*out)->stream);
+    if (e != cudaSuccess) {
+        destroy(*out);
+        *out = nullptr;
+        return cuda_fail(e, "clone");
+    }
+    return QS_OK;
+}
+
+void qs_register_free(qs_register* reg) { destroy(reg); }
+
+size_t qs_register_size(const qs_register* reg) { return reg ? size_t(reg->n) : 0; }
+
+int qs_register_precision(const qs_register* reg) { return reg ? reg->prec : -1; }
+
+int qs_register_set_arith(qs_register* reg, int arith) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (arith != QS_ARITH_EXACT && arith != QS_ARITH_FMA && arith != QS_ARITH_DF64)
+        return set_err(QS_INVALID_ARGUMENT, "unknown arithmetic mode");
+    reg->arith = arith;
+    return QS_OK;
+}
+
+int qs_try_apply_fast(qs_register* reg, const double* matrix, size_t rows, size_t cols, const size_t* targets,
+                      size_t k, size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    std::string msg;
+    int rc = qs::validate_gate(size_t(reg->n), rows, cols, targets, k, err, &msg);
+    if (rc) return set_err(rc, msg);
+    if (!matrix) return set_err(QS_INVALID_ARGUMENT, "matrix is null");
+    qs::OpDesc op;
+    qs::classify_gate(matrix, k, targets, &op);
+    rc = qs::apply_op(reg->state, reg->n, reg->prec, reg->arith, op, reg->stream, reg->sms, &msg);
+    return rc ? set_err(rc, msg) : QS_OK;
+}
+
+int qs_try_apply_all(qs_register* reg, const double* matrix, size_t rows, size_t cols, size_t k, size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (k != 1) {  // src/register.rs:269-271
+        if (err) err[0] = k;
+        return set_err(QS_INVALID_ARITY, "InvalidArity(" + std::to_string(k) + ")");
+    }
+    for (int q = 0; q < reg->n; q++) {
+        size_t t = size_t(q);
+        int rc = qs_try_apply_fast(reg, matrix, rows, cols, &t, 1, err);
+        if (rc) return rc;
+    }
+    return QS_OK;
+}
+
+int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m, const qs_circuit_options* opts,
+                     size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (m > 0 && !gates) return set_err(QS_INVALID_ARGUMENT, "gates is null");
+    qs_circuit_options o;
+    std::memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    std::vector<qs::OpDesc> ops(m);
+    std::string msg;
+    for (size_t g = 0; g < m; g++) {
+        const size_t dim = gates[g].k < 64 ? (size_t(1) << gates[g].k) : 0;
+        int rc = qs::validate_gate(size_t(reg->n), dim, dim, gates[g].targets, gates[g].k, err, &msg);
+        if (!rc && !gates[g].matrix) rc = QS_INVALID_ARGUMENT, msg = "matrix is null";
+        if (rc) {
+            if (err) err[2] = g;
+            return set_err(rc, "gate " + std::to_string(g) + ": " + msg);
+        }
+        qs::classify_gate(gates[g].matrix, gates[g].k, gates[g].targets, &ops[g]);
+    }
+    int rc = qs::run_circuit(reg->state, reg->n, reg->prec, reg->arith, ops, o, reg->stream, reg->sms, &msg);
+    return rc ? set_err(rc, msg) : QS_OK;
+}
+
+int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, double* prob0, double* prob1,
+                   size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (target >= size_t(reg->n)) {  // src/register.rs:299-301
+        if (err) err[0] = target;
+        return set_err(QS_INVALID_TARGET, "InvalidTarget(" + std::to_string(target) + ")");
+    }
+    QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(target), reg->partials, kMaxPartials,
+                                     reg->dres, reg->stream, reg->sms),
+            "measure_probs");
+    QS_CUDA(cudaMemcpyAsync(reg->hres, reg->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, reg->stream),
+            "measure readback");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "measure sync");
+    const double p0 = reg->hres[0], p1 = reg->hres[1];
+    const int res = draw > p0 ? 1 : 0;  // src/register.rs:321
+    const double total = res ? p1 : p0;  // :323
+    const double d = std::sqrt(total);
+    const double rinv = 1.0 / d;
+    QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, int(target), res, d, rinv, reg->stream, reg->sms),
+            "collapse");
+    if (outcome) *outcome = res;
+    if (prob0) *prob0 = p0;
+    if (prob1) *prob1 = p1;
+    return QS_OK;
+}
+
+int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, double* prob1, size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (target >= size_t(reg->n)) {
+        if (err) err[0] = target;
+        return set_err(QS_INVALID_TARGET, "InvalidTarget(" + std::to_string(target) + ")");
+    }
+    QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(target), reg->partials, kMaxPartials,
+                                     reg->dres, reg->stream, reg->sms),
+            "measure_probs");
+    QS_CUDA(cudaMemcpyAsync(reg->hres, reg->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, reg->stream),
+            "measure readback");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "measure sync");
+    if (prob0) *prob0 = reg->hres[0];
+    if (prob1) *prob1 = reg->hres[1];
+    return QS_OK;
+}
+
+uint64_t qs_launch_count(void) { return qs::g_launches.load(std::memory_order_relaxed); }
+
+int qs_get_state(const qs_register* reg, double* dst) {
+    if (!reg || !dst) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    const uint64_t N = 1ull << reg->n;
+    if (reg->prec == QS_PREC_C128) {
+        QS_CUDA(cudaMemcpyAsync(dst, reg->state, N * 16, cudaMemcpyDeviceToHost, reg->stream), "get_state");
+        QS_CUDA(cudaStreamSynchronize(reg->stream), "get_state sync");
+        return QS_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(N, 1ull << 22);
+    double* tmp = nullptr;
+    QS_CUDA(cudaMallocAsync((void**)&tmp, chunk * 16, reg->stream), "get_state temp");
+    for (uint64_t f = 0; f < N; f += chunk) {
+        const uint64_t c = std::min<uint64_t>(chunk, N - f);
+        QS_CUDA(qs::launch_to_c128(reg->state, reg->prec, f, c, tmp, reg->stream, reg->sms), "to_c128");
+        QS_CUDA(cudaMemcpyAsync(dst + 2 * f, tmp, c * 16, cudaMemcpyDeviceToHost, reg->stream), "get_state copy");
+    }
+    QS_CUDA(cudaFreeAsync(tmp, reg->stream), "get_state free");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "get_state sync");
+    return QS_OK;
+}
+
+int qs_set_state(qs_register* reg, const double* src) {
+    if (!reg || !src) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    const uint64_t N = 1ull << reg->n;
+    if (reg->prec == QS_PREC_C128) {
+        QS_CUDA(cudaMemcpyAsync(reg->state, src, N * 16, cudaMemcpyHostToDevice, reg->stream), "set_state");
+        QS_CUDA(cudaStreamSynchronize(reg->stream), "set_state sync");
+        return QS_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(N, 1ull << 22);
+    double* tmp = nullptr;
+    QS_CUDA(cudaMallocAsync((void**)&tmp, chunk * 16, reg->stream), "set_state temp");
+    for (uint64_t f = 0; f < N; f += chunk) {
+        const uint64_t c = std::min<uint64_t>(chunk, N - f);
+        QS_CUDA(cudaMemcpyAsync(tmp, src + 2 * f, c * 16, cudaMemcpyHostToDevice, reg->stream), "set_state copy");
+        QS_CUDA(qs::launch_from_c128(reg->state, reg->prec, f, c, tmp, reg->stream, reg->sms), "from_c128");
+    }
+    QS_CUDA(cudaFreeAsync(tmp, reg->stream), "set_state free");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "set_state sync");
+    return QS_OK;
+}
+
+int qs_probabilities(const qs_register* reg, double* dst) {
+    if (!reg || !dst) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    const uint64_t N = 1ull << reg->n;
+    const uint64_t chunk = std::min<uint64_t>(N, 1ull << 22);
+    double* tmp = nullptr;
+    QS_CUDA(cudaMallocAsync((void**)&tmp, chunk * 8, reg->stream), "probabilities temp");
+    for (uint64_t f = 0; f < N; f += chunk) {
+        const uint64_t c = std::min<uint64_t>(chunk, N - f);
+        QS_CUDA(qs::launch_norm_sqr(reg->state, reg->prec, f, c, tmp, reg->stream, reg->sms), "norm_sqr");
+        QS_CUDA(cudaMemcpyAsync(dst + f, tmp, c * 8, cudaMemcpyDeviceToHost, reg->stream), "probabilities copy");
+    }
+    QS_CUDA(cudaFreeAsync(tmp, reg->stream), "probabilities free");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "probabilities sync");
+    return QS_OK;
+}
+
+int qs_register_eq(const qs_register* a, const qs_register* b, double tol, int* equal) {
+    if (!a || !b || !equal) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    if (a->n != b->n || a->prec != b->prec) {
+        *equal = 0;
+        return QS_OK;
+    }
+    QS_CUDA(cudaStreamSynchronize(b->stream), "eq sync");
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(a->dres + 8);
+    QS_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), a->stream), "eq memset");
+    QS_CUDA(qs::launch_count_diff(a->state, b->state, a->n, a->prec, tol, cnt, a->stream, a->sms), "count_diff");
+    QS_CUDA(cudaMemcpyAsync(a->hres + 8, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, a->stream),
+            "eq readback");
+    QS_CUDA(cudaStreamSynchronize(a->stream), "eq sync");
+    unsigned long long c;
+    std::memcpy(&c, a->hres + 8, sizeof(c));
+    *equal = (c == 0);
+    return QS_OK;
+}
+
+int qs_synchronize(qs_register* reg) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    QS_CUDA(cudaStreamSynchronize(reg->stream), "synchronize");
+    return QS_OK;
+}
+
+void* qs_register_stream(qs_register* reg) { return reg ? (void*)reg->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// qs_circuit.cu — gate dispatch and the circuit runner.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qs_circuit.h"
+#include "qs_kernels.h"
+
+namespace qs {
+
+static int fail(cudaError_t e, const char* what, std::string* msg) {
+    if (msg) *msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return QS_OUT_OF_MEMORY;
+    }
+    return QS_CUDA_ERROR;
+}
+
+int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStream_t s, int sms, std::string* msg) {
+    if (op.kind == OP_NOOP) return QS_OK;
+    if (op.k <= kMaxSmallK) {
+        cudaError_t e = launch_op(op, state, n, prec, arith, s, sms);
+        return e == cudaSuccess ? QS_OK : fail(e, "gate kernel", msg);
+    }
+    if (op.k > kMaxBigK) {
+        if (msg) *msg = "dense or monomial sub-operation wider than " + std::to_string(kMaxBigK) + " qubits";
+        return QS_INVALID_ARGUMENT;
+    }
+    // Wide gate: tables in device memory, read the pre-gate state from a copy.
+    std::vector<uint64_t> off, off_src;
+    std::vector<uint8_t> pf;
+    std::vector<int8_t> lane;
+    std::vector<unsigned char> mat;
+    big_op_host_tables(op, prec, &off, &off_src, &pf, &lane, &mat);
+    const size_t amp = prec == QS_PREC_C64 ? 8 : 16;
+    const size_t sbytes = (size_t(1) << n) * amp;
+    unsigned char* blob = nullptr;
+    const size_t o_off = 0, o_src = o_off + off.size() * 8, o_pf = o_src + off_src.size() * 8,
+                 o_lane = o_pf + ((pf.size() + 15) / 16) * 16, o_mat = o_lane + ((lane.size() + 15) / 16) * 16,
+                 o_state = o_mat + ((mat.size() + 255) / 256) * 256, total = o_state + sbytes;
+    cudaError_t e = cudaMallocAsync((void**)&blob, total, s);
+    if (e != cudaSuccess) return fail(e, "wide gate buffers", msg);
+    BigOpBuffers b;
+    b.off = reinterpret_cast<const uint64_t*>(blob + o_off);
+    b.off_src = reinterpret_cast<const uint64_t*>(blob + o_src);
+    b.pf = blob + o_pf;
+    b.lane = reinterpret_cast<const int8_t*>(blob + o_lane);
+    b.mat = blob + o_mat;
+    if (!off.empty()) e = cudaMemcpyAsync(blob + o_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !off_src.empty())
+        e = cudaMemcpyAsync(blob + o_src, off_src.data(), off_src.size() * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !pf.empty()) e = cudaMemcpyAsync(blob + o_pf, pf.data(), pf.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !lane.empty())
+        e = cudaMemcpyAsync(blob + o_lane, lane.data(), lane.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !mat.empty()) e = cudaMemcpyAsync(blob + o_mat, mat.data(), mat.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(blob + o_state, state, sbytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = launch_op_big(op, state, blob + o_state, n, prec, arith, b, s, sms);
+    cudaFreeAsync(blob, s);
+    return e == cudaSuccess ? QS_OK : fail(e, "wide gate", msg);
+}
+
+int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
+                const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
+    (void)opts;
+    for (size_t g = 0; g < ops.size(); g++) {
+        int rc = apply_op(state, n, prec, arith, ops[g], s, sms, msg);
+        if (rc) return rc;
+    }
+    return QS_OK;
+}
+
+}  // namespace qs

@@ -1,0 +1,58 @@
+// qs_kernels.h — host-callable launchers of the engine's kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+constexpr uint8_t PF_SKIP_DEV = 4;  // PfClass::PF_SKIP as seen by device code
+
+// Count kernel launches made by this library (read back through qs_launch_count).
+void note_launches(uint64_t count);
+
+// Device tables of a sub-operation wider than kMaxSmallK qubits.
+struct BigOpBuffers {
+    const uint64_t* off = nullptr;
+    const uint64_t* off_src = nullptr;
+    const uint8_t* pf = nullptr;
+    const int8_t* lane = nullptr;
+    const void* mat = nullptr;  // dense matrix or monomial phases, in the state's real type
+};
+
+// One sweep applying `op` (op.k <= kMaxSmallK) in place.
+cudaError_t launch_op(const OpDesc& op, void* state, int n, int prec, int arith, cudaStream_t s, int sms);
+
+// One sweep applying a wide `op`, reading the pre-gate state from `src`.
+cudaError_t launch_op_big(const OpDesc& op, void* state, const void* src, int n, int prec, int arith,
+                          const BigOpBuffers& b, cudaStream_t s, int sms);
+
+// Host images of the tables launch_op_big reads.
+void big_op_host_tables(const OpDesc& op, int prec, std::vector<uint64_t>* off, std::vector<uint64_t>* off_src,
+                        std::vector<uint8_t>* pf, std::vector<int8_t>* lane, std::vector<unsigned char>* mat);
+
+// ---- state-wide kernels (qs_state.cu) ----
+cudaError_t launch_init_basis(void* state, int n, int prec, uint64_t index, cudaStream_t s, int sms);
+cudaError_t launch_init_product(void* state, int n, int prec, const double* qubits, cudaStream_t s, int sms);
+// FP64 probability sums of target bit 0 / 1 into out[0], out[1] (device), via per-block partials.
+cudaError_t launch_measure_probs(const void* state, int n, int prec, int target, double* partials,
+                                 int max_partials, double* out, cudaStream_t s, int sms);
+// Zero amplitudes whose target bit != outcome and divide the rest by d (rinv = 1/d).
+cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
+                            cudaStream_t s, int sms);
+// norm_sqr of amplitudes [first, first + count) into dst (device).
+cudaError_t launch_norm_sqr(const void* state, int prec, uint64_t first, uint64_t count, double* dst,
+                            cudaStream_t s, int sms);
+// Convert amplitudes [first, first+count) between the state's type and interleaved doubles.
+cudaError_t launch_to_c128(const void* state, int prec, uint64_t first, uint64_t count, double* dst,
+                           cudaStream_t s, int sms);
+cudaError_t launch_from_c128(void* state, int prec, uint64_t first, uint64_t count, const double* src,
+                             cudaStream_t s, int sms);
+// Count amplitudes with |a_i - b_i| >= tol (hypot, as num-complex's norm) into *count (device).
+cudaError_t launch_count_diff(const void* a, const void* b, int n, int prec, double tol,
+                              unsigned long long* count, cudaStream_t s, int sms);
+
+}  // namespace qs

@@ -1,0 +1,255 @@
+"""Quaru's Register (src/register.rs) backed by a GB300 state vector.
+
+Same names, argument meaning and error behaviour as the reference: the
+try_* methods raise OperationError (the Rust Result's Err), the plain methods
+are the panicking forms. measure() takes the uniform draw from a
+caller-supplied generator because the reference's thread_rng
+(src/register.rs:317-318) cannot be seeded; by default numpy's generator is
+used.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Callable, Iterable, Sequence
+
+import numpy as np
+
+from . import _lib
+from .operation import Operation
+
+
+class OperationError(Exception):
+    """src/register.rs:10-20. kind is one of InvalidTarget, InvalidDimensions, InvalidArity, InvalidQubit."""
+
+    KINDS = {_lib.QS_INVALID_TARGET: "InvalidTarget", _lib.QS_INVALID_DIMENSIONS: "InvalidDimensions",
+             _lib.QS_INVALID_ARITY: "InvalidArity", _lib.QS_INVALID_QUBIT: "InvalidQubit"}
+
+    def __init__(self, code: int, payload: tuple, message: str = ""):
+        self.code = code
+        self.kind = self.KINDS.get(code, "Other")
+        self.payload = payload
+        super().__init__(f"{self.kind}{payload} {message}".strip())
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, OperationError) and (self.code, self.payload) == (other.code, other.payload)
+
+    def __hash__(self):
+        return hash((self.code, self.payload))
+
+
+class EngineError(RuntimeError):
+    """A device-side failure (CUDA error, out of memory, timeout) or a bad argument."""
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _sp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_size_t))
+
+
+def _check(rc: int, err: np.ndarray | None = None) -> None:
+    if rc == _lib.QS_OK:
+        return
+    msg = _lib.last_error()
+    if rc in OperationError.KINDS:
+        if rc == _lib.QS_INVALID_DIMENSIONS:
+            payload = (int(err[0]), int(err[1]))
+        else:
+            payload = (int(err[0]),) if err is not None else ()
+        raise OperationError(rc, payload, msg)
+    raise EngineError(f"quaru_gb300 error {rc}: {msg}")
+
+
+def _matrix(m) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+
+
+class Register:
+    """A quantum register of n qubits whose state lives in GPU memory (src/register.rs:22-37)."""
+
+    def __init__(self, handle: int, rng: Callable[[], float] | None = None):
+        self._h = ctypes.c_void_p(handle)
+        self._rng = rng or np.random.default_rng().random
+
+    # ---- construction (src/register.rs:41-102)
+    @classmethod
+    def new(cls, input_bits: Sequence[bool], precision: int = _lib.QS_PREC_C128, rng=None) -> "Register":
+        lib = _lib.load()
+        b = np.ascontiguousarray(np.array([1 if x else 0 for x in input_bits], dtype=np.uint8))
+        h = ctypes.c_void_p()
+        _check(lib.qs_register_new(b.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), len(b), precision,
+                                   ctypes.byref(h)))
+        return cls(h.value, rng)
+
+    @classmethod
+    def from_int(cls, n: int, k: int, precision: int = _lib.QS_PREC_C128, rng=None) -> "Register":
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(lib.qs_register_from_int(n, k, precision, ctypes.byref(h)))
+        return cls(h.value, rng)
+
+    @classmethod
+    def try_from_qubits(cls, qubits, precision: int = _lib.QS_PREC_C128, rng=None) -> "Register":
+        lib = _lib.load()
+        q = np.ascontiguousarray(np.array([np.asarray(x, dtype=np.complex128).ravel() for x in qubits]))
+        if q.size and q.shape[1] != 2:
+            raise OperationError(_lib.QS_INVALID_QUBIT, (0,), "each qubit needs 2 amplitudes")
+        err = np.zeros(3, dtype=np.uintp)
+        h = ctypes.c_void_p()
+        _check(lib.qs_register_try_from_qubits(_dp(q.view(np.float64)), q.shape[0], precision, ctypes.byref(h),
+                                               _sp(err)), err)
+        return cls(h.value, rng)
+
+    @classmethod
+    def from_qubits(cls, qubits, precision: int = _lib.QS_PREC_C128, rng=None) -> "Register":
+        try:
+            return cls.try_from_qubits(qubits, precision, rng)
+        except OperationError as e:
+            raise RuntimeError("Incorrect input qubits") from e
+
+    def clone(self) -> "Register":
+        h = ctypes.c_void_p()
+        _check(_lib.load().qs_register_clone(self._h, ctypes.byref(h)))
+        return Register(h.value, self._rng)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.qs_register_free(h)
+            self._h = ctypes.c_void_p()
+
+    # ---- properties
+    def size(self) -> int:
+        return int(_lib.load().qs_register_size(self._h))
+
+    @property
+    def precision(self) -> int:
+        return int(_lib.load().qs_register_precision(self._h))
+
+    def set_arith(self, arith: int) -> None:
+        _check(_lib.load().qs_register_set_arith(self._h, arith))
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(_lib.load().qs_register_stream(self._h) or 0)
+
+    # ---- gate application (src/register.rs:134-191, 259-281)
+    def try_apply_fast(self, op: Operation) -> "Register":
+        m = _matrix(op.matrix)
+        t = np.ascontiguousarray(np.array(list(op.targets), dtype=np.uintp))
+        err = np.zeros(3, dtype=np.uintp)
+        rows = m.shape[0]
+        cols = m.shape[1] if m.ndim == 2 else 1
+        _check(_lib.load().qs_try_apply_fast(self._h, _dp(m.view(np.float64)), rows, cols, _sp(t), len(t),
+                                             _sp(err)), err)
+        return self
+
+    try_apply = try_apply_fast
+
+    def apply(self, op: Operation) -> "Register":
+        try:
+            return self.try_apply_fast(op)
+        except OperationError as e:
+            raise RuntimeError("Could not apply operation") from e
+
+    def try_apply_all(self, op: Operation) -> "Register":
+        m = _matrix(op.matrix)
+        err = np.zeros(3, dtype=np.uintp)
+        _check(_lib.load().qs_try_apply_all(self._h, _dp(m.view(np.float64)), m.shape[0], m.shape[1],
+                                            op.arity(), _sp(err)), err)
+        return self
+
+    def apply_all(self, op: Operation) -> "Register":
+        try:
+            return self.try_apply_all(op)
+        except OperationError as e:
+            raise RuntimeError("Could not apply operation") from e
+
+    def apply_gates(self, ops: Iterable[Operation], fuse: int = 0, max_width: int = 5, tile_qubits: int = 0):
+        """The operations loop of apply_circuit (src/register.rs:346-350) in one library call."""
+        ops = list(ops)
+        keep = []
+        gates = (_lib.QsGate * max(1, len(ops)))()
+        for i, op in enumerate(ops):
+            m = _matrix(op.matrix)
+            t = np.ascontiguousarray(np.array(list(op.targets), dtype=np.uintp))
+            keep += [m, t]
+            gates[i].k = len(t)
+            gates[i].targets = _sp(t)
+            gates[i].matrix = _dp(m.view(np.float64))
+        opts = _lib.QsCircuitOptions(fuse, max_width, tile_qubits, 0)
+        err = np.zeros(3, dtype=np.uintp)
+        rc = _lib.load().qs_apply_circuit(self._h, gates, len(ops), ctypes.byref(opts), _sp(err))
+        _check(rc, err)
+        return self
+
+    # ---- measurement (src/register.rs:291-342)
+    def try_measure(self, target: int, draw: float | None = None) -> bool:
+        x = self._rng() if draw is None else float(draw)
+        out = ctypes.c_int(0)
+        p0, p1 = ctypes.c_double(0), ctypes.c_double(0)
+        err = np.zeros(3, dtype=np.uintp)
+        _check(_lib.load().qs_try_measure(self._h, target, x, ctypes.byref(out), ctypes.byref(p0), ctypes.byref(p1),
+                                          _sp(err)), err)
+        self.last_probs = (p0.value, p1.value)
+        return bool(out.value)
+
+    def measure(self, target: int, draw: float | None = None) -> bool:
+        try:
+            return self.try_measure(target, draw)
+        except OperationError as e:
+            raise RuntimeError("Could not measure bit") from e
+
+    # ---- host views (src/register.rs:35, 379-413)
+    @property
+    def state(self) -> np.ndarray:
+        st = np.zeros(1 << self.size(), dtype=np.complex128)
+        _check(_lib.load().qs_get_state(self._h, _dp(st.view(np.float64))))
+        return st
+
+    @state.setter
+    def state(self, value) -> None:
+        v = np.ascontiguousarray(np.asarray(value, dtype=np.complex128).ravel())
+        if v.size != 1 << self.size():
+            raise ValueError("state has the wrong length")
+        _check(_lib.load().qs_set_state(self._h, _dp(v.view(np.float64))))
+
+    def probabilities(self) -> np.ndarray:
+        p = np.zeros(1 << self.size(), dtype=np.float64)
+        _check(_lib.load().qs_probabilities(self._h, _dp(p)))
+        return p
+
+    def print_probabilities(self) -> None:
+        n = self.size()
+        for i, p in enumerate(self.probabilities()):
+            print(f"{i:0{n}b}: {p * 100.0}%")
+
+    def print_nonzero_probabilities(self) -> None:
+        n = self.size()
+        for i, p in enumerate(self.probabilities()):
+            if p > 0.0:
+                print(f"{i:0{n}b}: {p * 100.0}%")
+
+    def print_state(self) -> None:
+        n = self.size()
+        for i, s in enumerate(self.state):
+            print(f"{i:0{n}b}: {s}")
+
+    def eq(self, other: "Register", tol: float = 1e-8) -> bool:
+        e = ctypes.c_int(0)
+        _check(_lib.load().qs_register_eq(self._h, other._h, tol, ctypes.byref(e)))
+        return bool(e.value)
+
+    def __eq__(self, other) -> bool:  # PartialEq, src/register.rs:409-413
+        return isinstance(other, Register) and self.eq(other, 1e-8)
+
+    __hash__ = None
+
+    def synchronize(self) -> None:
+        _check(_lib.load().qs_synchronize(self._h))
