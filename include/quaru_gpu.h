@@ -139,6 +139,26 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
  * FP64 on the GPU. The state is left unchanged. */
 int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, double* prob1, size_t* err);
 
+/* For callers that cannot allocate device memory. No counterpart in the
+ * reference: Quaru's Register always owns its state. Code that runs under a
+ * framework's own allocator, inside a fixed pre-planned memory budget, or on
+ * a path where cudaMalloc and its implicit synchronisation are not allowed
+ * keeps its state vector in a buffer it allocated itself (2^n amplitudes,
+ * interleaved complex128 or complex64 per `precision`) and gets the
+ * probability sums of try_measure for it here. out is a device pointer to 2
+ * doubles (prob_0, prob_1); work is queued on `stream` (a cudaStream_t, null =
+ * default stream) and out is valid once that stream reaches it. The sums equal
+ * those of qs_measure_probabilities for the same amplitudes.
+ * Allocates nothing: per-block partial sums go to a 64 KiB file-scope
+ * __device__ array that every GPU loading this library holds until exit, so
+ * any n in 1..40 fits; a request needing more scratch than that is rejected
+ * with QS_INVALID_ARGUMENT. The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. Every call shares the array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised. */
+int qs_measure_probabilities_noalloc(const void* state, size_t n, int precision, size_t target,
+                                     double* out, void* stream, size_t* err);
+
 /* ---- host views ---------------------------------------------------------- */
 
 /* Read `pub state` (src/register.rs:35): 2^n complex, interleaved doubles. */

@@ -62,6 +62,7 @@ SIGNATURES = {
     "qs_apply_circuit": (_i, [_vp, _P(QsGate), _sz, _P(QsCircuitOptions), _sp]),
     "qs_try_measure": (_i, [_vp, _sz, ctypes.c_double, _P(_i), _dp, _dp, _sp]),
     "qs_measure_probabilities": (_i, [_vp, _sz, _dp, _dp, _sp]),
+    "qs_measure_probabilities_noalloc": (_i, [_vp, _sz, _i, _sz, _vp, _vp, _sp]),
     "qs_get_state": (_i, [_vp, _dp]),
     "qs_set_state": (_i, [_vp, _dp]),
     "qs_probabilities": (_i, [_vp, _dp]),

@@ -104,6 +104,10 @@ int allocate(size_t n, int prec, qs_register** out) {
 
 }  // namespace
 
+namespace qs {
+void set_last_error_message(const std::string& msg) { g_last_error = msg; }
+}  // namespace qs
+
 extern "C" {
 
 const char* qs_last_error(void) { return g_last_error.c_str(); }

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "qs_internal.h"
@@ -13,6 +14,9 @@ constexpr uint8_t PF_SKIP_DEV = 4;  // PfClass::PF_SKIP as seen by device code
 
 // Count kernel launches made by this library (read back through qs_launch_count).
 void note_launches(uint64_t count);
+
+// Set the message qs_last_error() returns on the calling thread.
+void set_last_error_message(const std::string& msg);
 
 // Device tables of a sub-operation wider than kMaxSmallK qubits.
 struct BigOpBuffers {
