@@ -108,3 +108,65 @@ __device__ __forceinline__ T apply_pf(T x, uint8_t cls) {
 }
 
 }  // namespace qs
+
+namespace qs {
+
+// ---- double-float arithmetic on the FP32 pipe (QS_ARITH_DF64) ------------
+// GB300's FP64 rate (~2 FMA/clk/SM) cannot keep up with HBM for dense gates;
+// its FP32 rate can. A double x is carried as floats (h, l) with
+// x = h + l + d, |d| <= 2^-47 |x|; sums of products use Dekker/Knuth
+// error-free transformations (TwoProduct by FMA, TwoSum), and the result is
+// rejoined by one FP64 addition. Valid for 2^-126 <= |x| < 2^128; smaller
+// magnitudes are flushed (absolute error < 2^-74 |x|... below 2^-126).
+
+// Split with integer operations only: h is x with its significand truncated
+// to 24 bits, l is the remaining 29 bits rounded to 24 bits.
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+    const uint32_t hi = uint32_t(__double2hiint(x)), lo = uint32_t(__double2loint(x));
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    const uint32_t sign = hi & 0x80000000u;
+    const uint32_t hb = ((__funnelshift_l(lo, hi, 3) - 0xC0000000u) & 0x7fffffffu) | sign;
+    const uint32_t sb = (e * 0x800000u - 948u * 0x800000u) | sign;  // +-2^(e-1075), for e >= 949
+    const float lf = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), __uint_as_float(sb));
+    h = (e >= 897u) ? __uint_as_float(hb) : 0.0f;
+    l = (e >= 949u) ? lf : 0.0f;
+}
+
+// Exact float -> double conversion with integer operations (floats below
+// 2^-126 flush to zero).
+__device__ __forceinline__ double df_f2d(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t mag = b & 0x7fffffffu;
+    const uint32_t hi = ((mag >> 3) + (896u << 20)) | (b & 0x80000000u);
+    return (mag >= 0x00800000u) ? __hiloint2double(int(hi), int(b << 29)) : 0.0;
+}
+
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// sum_{k<NT} (uh_k + ul_k) * (xh_k + xl_k), returned as a double.
+template <int NT>
+__device__ __forceinline__ double df_dot(const float* uh, const float* ul, const float* xh, const float* xl) {
+    float p[NT];
+    float c = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        p[k] = __fmul_rn(uh[k], xh[k]);
+        c = __fadd_rn(c, __fmaf_rn(uh[k], xh[k], -p[k]));
+        c = __fmaf_rn(uh[k], xl[k], c);
+        c = __fmaf_rn(ul[k], xh[k], c);
+    }
+    float s = p[0];
+#pragma unroll
+    for (int k = 1; k < NT; k++) {
+        float t;
+        df_two_sum(s, p[k], s, t);
+        c = __fadd_rn(c, t);
+    }
+    return __dadd_rn(df_f2d(s), df_f2d(c));
+}
+
+}  // namespace qs

@@ -30,9 +30,17 @@ struct Dense1Args {
     IndexMap map;
     uint64_t tbit;  // 1 << target
     R m[8];         // u00, u01, u10, u11 interleaved
+    // QS_ARITH_DF64: per output (y0.re, y0.im, y1.re, y1.im) four coefficients
+    // (sign folded in) as float pairs, applied to the inputs listed in kDfIn.
+    float dfh[16];
+    float dfl[16];
 };
 
-// MODE 0: exact complex, 1: exact real, 2: FMA complex, 3: FMA real.
+// DF64 term t of output o multiplies input component (x0.re, x0.im, x1.re,
+// x1.im = 0..3) number t for real outputs and t ^ 1 for imaginary outputs.
+
+// MODE 0: exact complex, 1: exact real, 2: FMA complex, 3: FMA real,
+// 4: double-float complex, 5: double-float real (complex128 only).
 template <typename R, int MODE, int ILP>
 __global__ void __launch_bounds__(kThreads) k_dense1(typename Cplx<R>::T* __restrict__ st, uint64_t ntup,
                                                      const __grid_constant__ Dense1Args<R> a) {
@@ -60,6 +68,36 @@ __global__ void __launch_bounds__(kThreads) k_dense1(typename Cplx<R>::T* __rest
             } else if constexpr (MODE == 1) {
                 y0 = cadd_exact(cmul_exact_real(a.m[0], x0[u]), cmul_exact_real(a.m[2], x1[u]));
                 y1 = cadd_exact(cmul_exact_real(a.m[4], x0[u]), cmul_exact_real(a.m[6], x1[u]));
+            } else if constexpr (MODE == 4 || MODE == 5) {
+                float xh[4], xl[4];
+                df_split(x0[u].x, xh[0], xl[0]);
+                df_split(x0[u].y, xh[1], xl[1]);
+                df_split(x1[u].x, xh[2], xl[2]);
+                df_split(x1[u].y, xh[3], xl[3]);
+                double out[4];
+#pragma unroll
+                for (int o = 0; o < 4; o++) {
+                    if constexpr (MODE == 4) {
+                        float th[4], tl[4];
+#pragma unroll
+                        for (int t = 0; t < 4; t++) {
+                            th[t] = xh[(o & 1) ? (t ^ 1) : t];
+                            tl[t] = xl[(o & 1) ? (t ^ 1) : t];
+                        }
+                        out[o] = df_dot<4>(a.dfh + 4 * o, a.dfl + 4 * o, th, tl);
+                    } else {
+                        // real matrix: y.re uses x.re terms 0 and 2, y.im uses x.im terms
+                        const float th[2] = {xh[(o & 1)], xh[2 + (o & 1)]};
+                        const float tl[2] = {xl[(o & 1)], xl[2 + (o & 1)]};
+                        const float ch[2] = {a.dfh[4 * o], a.dfh[4 * o + 2]};  // u.re of columns 0 and 1
+                        const float cl[2] = {a.dfl[4 * o], a.dfl[4 * o + 2]};
+                        out[o] = df_dot<2>(ch, cl, th, tl);
+                    }
+                }
+                y0.x = out[0];
+                y0.y = out[1];
+                y1.x = out[2];
+                y1.y = out[3];
             } else if constexpr (MODE == 2) {
                 y0 = cfma(a.m[2], a.m[3], x1[u], czero<T>());
                 y0 = cfma(a.m[0], a.m[1], x0[u], y0);
@@ -299,8 +337,38 @@ static int grid_for(uint64_t work, int num_sms, int per_thread = 1) {
     return int(blocks);
 }
 
+// Split the 2x2 matrix into the float-pair coefficients of the DF64 modes.
+// Returns false when an entry is outside the range double-float handles.
 template <typename R>
-static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms) {
+static bool fill_df64(Dense1Args<R>& a) {
+    // coefficient of term t of output o: (row, column, part, sign); inputs follow kDfIn
+    const int row[4] = {0, 0, 1, 1};
+    for (int o = 0; o < 4; o++) {
+        const bool im_out = o & 1;
+        for (int t = 0; t < 4; t++) {
+            const int col = t >> 1;           // terms 0,1 -> x0 ; 2,3 -> x1
+            const bool cross = (t & 1) != 0;  // term uses the other component of x
+            // re out: u.re * x.re (t even), -u.im * x.im (t odd)
+            // im out: u.re * x.im (t even),  u.im * x.re (t odd)
+            double v;
+            const int idx = 2 * (row[o] * 2 + col);
+            if (!cross)
+                v = double(a.m[idx]);
+            else
+                v = im_out ? double(a.m[idx + 1]) : -double(a.m[idx + 1]);
+            const double av = v < 0 ? -v : v;
+            if (av != 0.0 && (av > 0x1p100 || av < 0x1p-100)) return false;
+            const float h = float(v);
+            a.dfh[4 * o + t] = h;
+            a.dfl[4 * o + t] = float(v - double(h));
+        }
+    }
+    return true;
+}
+
+template <typename R>
+static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms,
+                                 bool df64 = false) {
     using T = typename Cplx<R>::T;
     Dense1Args<R> a;
     std::memset(&a, 0, sizeof(a));
@@ -318,6 +386,13 @@ static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exac
                 k_dense1<R, 1, ILP><<<grid, kThreads, 0, s>>>(st, ntup, a);
             else
                 k_dense1<R, 0, ILP><<<grid, kThreads, 0, s>>>(st, ntup, a);
+            return counted(cudaGetLastError());
+        }
+        if (df64 && fill_df64(a)) {
+            if (real)
+                k_dense1<R, 5, 1><<<grid_for(ntup, sms, 1), kThreads, 0, s>>>(st, ntup, a);
+            else
+                k_dense1<R, 4, 1><<<grid_for(ntup, sms, 1), kThreads, 0, s>>>(st, ntup, a);
             return counted(cudaGetLastError());
         }
     }
@@ -380,7 +455,8 @@ static cudaError_t launch_mono(const OpDesc& op, void* state, int n, cudaStream_
 }
 
 template <typename R>
-static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms) {
+static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms,
+                                bool df64 = false) {
     if (op.kind == OP_MONO || op.kind == OP_MONO_PF) {
         switch (op.k) {
             case 0: return launch_mono<R, 0>(op, state, n, s, sms);
@@ -403,7 +479,7 @@ static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact
                 z.pf[0] = 255;
                 return launch_mono<R, 0>(z, state, n, s, sms);
             }
-            case 1: return launch_dense1<R>(op, state, n, exact, s, sms);
+            case 1: return launch_dense1<R>(op, state, n, exact, s, sms, df64);
             case 2: return launch_denseK<R, 2>(op, state, n, exact, s, sms);
             case 3: return launch_denseK<R, 3>(op, state, n, exact, s, sms);
             case 4: return launch_denseK<R, 4>(op, state, n, exact, s, sms);
@@ -418,7 +494,7 @@ cudaError_t launch_op(const OpDesc& op, void* state, int n, int prec, int arith,
     if (op.k > kMaxSmallK) return cudaErrorInvalidValue;
     const bool exact = (arith == QS_ARITH_EXACT);
     if (prec == QS_PREC_C64) return launch_small<float>(op, state, n, false, s, sms);
-    return launch_small<double>(op, state, n, exact, s, sms);
+    return launch_small<double>(op, state, n, exact, s, sms, arith == QS_ARITH_DF64);
 }
 
 cudaError_t launch_op_big(const OpDesc& op, void* state, const void* src, int n, int prec, int arith,

@@ -59,6 +59,10 @@ def test_gpu_fma_and_c64_within_tolerance():
     reg.set_arith(q.QS_ARITH_FMA)
     reg.apply_gates(gates)
     assert floored_rel_err(reg.state, ref) <= 1e-12
+    rdf = q.Register.from_int(doc["n"], 0)
+    rdf.set_arith(q.QS_ARITH_DF64)
+    rdf.apply_gates(gates)
+    assert floored_rel_err(rdf.state, ref) <= 1e-12
     r64 = q.Register.from_int(doc["n"], 0, precision=q.QS_PREC_C64)
     r64.apply_gates(gates)
     assert floored_rel_err(r64.state, ref) <= 1e-4

@@ -287,3 +287,35 @@ def test_error_codes(q):
         g.apply_gates([O.hadamard(0), O.cnot(0, 9)])
     assert e.value.payload == (9,)
     assert np.array_equal(g.state, q.Register.new([False] * 4).state)  # nothing applied
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 12])
+def test_df64_random_circuits_within_tolerance(q, orc, n):
+    from quaru_gb300.workloads import config1_circuit
+
+    c = config1_circuit(n=max(n, 3), m=400, seed=300 + n) if n >= 3 else None
+    rng = np.random.default_rng(310 + n)
+    if c is None:
+        from quaru_gb300.operation import Operation
+
+        ops = [Operation(rand_unitary(rng, 1), [int(rng.integers(n))]) for _ in range(200)]
+        nn = n
+    else:
+        ops, nn = c.gates, c.n
+    o, g = run_pair(q, orc, nn, ops, arith=2, state=rand_state(rng, nn))
+    assert floored_rel_err(g, o) <= 1e-12
+
+
+def test_df64_deep_layered_circuit(q, orc):
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    n = 14
+    ops = flatten(layered_circuit(n, 30, 99))
+    o, g = run_pair(q, orc, n, ops, arith=2)
+    assert floored_rel_err(g, o) <= 1e-12
+    # tiny amplitudes (down to 1e-30) stay within the floored bound too
+    rng = np.random.default_rng(12)
+    st = rand_state(rng, 10) * np.logspace(0, -30, 1 << 10)
+    st /= np.linalg.norm(st)
+    o, g = run_pair(q, orc, 10, flatten(layered_circuit(10, 5, 7)), arith=2, state=st)
+    assert floored_rel_err(g, o) <= 1e-12
