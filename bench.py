@@ -266,6 +266,23 @@ def run_ours(args) -> None:
         e2e_s = time.perf_counter() - t0
     clk = clocks.summary()
 
+    fused = None
+    if args.fused:
+        # The same layers through qs_apply_circuit with cache-blocked stages.
+        fl = [g for i in range(args.warmup, args.warmup + args.steps) for g in layer(i)]
+        reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=1)
+        barrier()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        l0 = lib.qs_launch_count()
+        f0.record(stream)
+        reg.apply_gates(fl, fuse=1)
+        f1.record(stream)
+        barrier()
+        fs = f0.elapsed_time(f1) / 1e3
+        fused = {"gates_per_s": len(fl) / fs, "ms_per_step": 1e3 * fs / args.steps,
+                 "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0)}
+
     t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -317,6 +334,7 @@ def run_ours(args) -> None:
                                    "frac": flops_per_launch / avg_haar_s / 1e12 / FP64_PEAK_TFLOPS_MEASURED}},
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
         "clocks": clk,
+        "fused": fused,
         "cpu_baseline": cpu,
         "probe": {"p0_qubit0": p0},
     }
@@ -348,6 +366,7 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-qubits", type=int, default=26)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fused", action="store_true", help="also time the fused (tiled) circuit path")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")

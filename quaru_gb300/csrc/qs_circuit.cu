@@ -1,12 +1,14 @@
 // qs_circuit.cu — gate dispatch and the circuit runner.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "qs_circuit.h"
 #include "qs_kernels.h"
+#include "qs_tile.h"
 
 namespace qs {
 
@@ -64,7 +66,15 @@ int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStre
 
 int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
                 const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
-    (void)opts;
+    if (opts.fuse >= 1) {
+        // Tile qubits: 32 KiB of shared memory per tile by default.
+        int T = opts.tile_qubits > 0 ? opts.tile_qubits : (prec == QS_PREC_C64 ? 12 : 11);
+        T = std::min(T, n);
+        const int L = std::min(5, T);
+        std::vector<TileStage> stages =
+            plan_tiles(ops, n, T, L, prec == QS_PREC_C128 && arith == QS_ARITH_EXACT);
+        return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg);
+    }
     for (size_t g = 0; g < ops.size(); g++) {
         int rc = apply_op(state, n, prec, arith, ops[g], s, sms, msg);
         if (rc) return rc;

@@ -170,3 +170,30 @@ __device__ __forceinline__ double df_dot(const float* uh, const float* ul, const
 }
 
 }  // namespace qs
+
+namespace qs {
+
+// As df_dot, but returns the sum as a normalised float pair (h, l) (TwoSum).
+template <int NT>
+__device__ __forceinline__ void df_dot_pair(const float* uh, const float* ul, const float* xh, const float* xl,
+                                            float& h, float& l) {
+    float p[NT];
+    float c = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        p[k] = __fmul_rn(uh[k], xh[k]);
+        c = __fadd_rn(c, __fmaf_rn(uh[k], xh[k], -p[k]));
+        c = __fmaf_rn(uh[k], xl[k], c);
+        c = __fmaf_rn(ul[k], xh[k], c);
+    }
+    float s = p[0];
+#pragma unroll
+    for (int k = 1; k < NT; k++) {
+        float t;
+        df_two_sum(s, p[k], s, t);
+        c = __fadd_rn(c, t);
+    }
+    df_two_sum(s, c, h, l);
+}
+
+}  // namespace qs

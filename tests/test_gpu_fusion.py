@@ -1,0 +1,112 @@
+"""Cache-blocked stages (fuse=1) against gate-by-gate application and the oracle.
+
+Under QS_ARITH_EXACT a fused run must be bit-identical to the unfused run (the
+tile kernel applies each gate with the same arithmetic); FMA and DF64 stay
+within 1e-12 of the FP64 oracle, complex64 within 1e-4.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from tests.fixtures import floored_rel_err, value_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_unitary(rng, k):
+    d = 1 << k
+    z = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) / math.sqrt(2)
+    qm, r = np.linalg.qr(z)
+    return qm * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def mixed_circuit(rng, n, m):
+    from quaru_gb300 import operation as O
+    from quaru_gb300.operation import Operation
+    from quaru_gb300.workloads import SplitMix64, random_gate
+
+    sm = SplitMix64(int(rng.integers(1 << 30)))
+    ops = [random_gate(sm, n) for _ in range(m)]
+    # extra structure: controlled dense gates, 0-controls, a wide gate and a dense 2-qubit gate
+    for _ in range(6):
+        a, b, c = (int(x) for x in rng.permutation(n)[:3])
+        ops.insert(int(rng.integers(len(ops))), O.to_controlled(Operation(rand_unitary(rng, 1), [a]), b))
+        ops.insert(int(rng.integers(len(ops))), O.cnx([b, c], a))
+    ops.insert(len(ops) // 2, Operation(rand_unitary(rng, 2), [int(x) for x in rng.permutation(n)[:2]]))
+    if n >= 7:
+        ops.insert(len(ops) // 3, Operation(rand_unitary(rng, 6), [int(x) for x in rng.permutation(n)[:6]]))
+    return ops
+
+
+@pytest.mark.parametrize("n", [4, 11, 12, 15, 20])
+def test_fused_exact_bit_identical(n):
+    import quaru_gb300 as q
+
+    rng = np.random.default_rng(1000 + n)
+    ops = mixed_circuit(rng, n, 300)
+    a = q.Register.from_int(n, 0)
+    a.apply_gates(ops, fuse=0)
+    b = q.Register.from_int(n, 0)
+    b.apply_gates(ops, fuse=1)
+    assert value_equal(a.state, b.state)
+    if n >= 12:
+        c = q.Register.from_int(n, 0)
+        c.apply_gates(ops, fuse=1, tile_qubits=8)
+        assert value_equal(a.state, c.state)
+
+
+@pytest.mark.parametrize("arith", [1, 2])
+def test_fused_fma_df64_within_tolerance(arith):
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    n = 16
+    ops = flatten(layered_circuit(n, 12, 4242)) + mixed_circuit(np.random.default_rng(5), n, 100)
+    o = OracleRegister.from_int(n, 0)
+    o.apply_sequence([(g.matrix, g.targets) for g in ops])
+    g = q.Register.from_int(n, 0)
+    g.set_arith(arith)
+    g.apply_gates(ops, fuse=1)
+    assert floored_rel_err(g.state, o.state) <= 1e-12
+
+
+def test_fused_c64_within_tolerance():
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    n = 15
+    ops = flatten(layered_circuit(n, 10, 77))
+    o = OracleRegister.from_int(n, 0)
+    o.apply_sequence([(g.matrix, g.targets) for g in ops])
+    g = q.Register.from_int(n, 0, precision=1)
+    g.apply_gates(ops, fuse=1)
+    assert floored_rel_err(g.state, o.state) <= 1e-4
+    h = q.Register.from_int(n, 0, precision=1)
+    h.apply_gates(ops, fuse=0)
+    assert floored_rel_err(g.state, h.state) <= 1e-5
+
+
+def test_fused_large_state_permutation_round_trip_bit_exact():
+    """24 qubits: a permutation-and-phase circuit followed by its inverse restores the state exactly."""
+    import quaru_gb300 as q
+    from quaru_gb300 import operation as O
+
+    n = 24
+    rng = np.random.default_rng(9)
+    ops = []
+    for _ in range(200):
+        a, b, c = (int(x) for x in rng.permutation(n)[:3])
+        ops += [O.cnot(a, b), O.swap(b, c), O.cnx([a, c], b), O.pauli_y(c), O.not_(a)]
+    inv = []
+    for g in reversed(ops):
+        inv.append(O.Operation(np.ascontiguousarray(np.asarray(g.matrix).conj().T), g.targets))
+    reg = q.Register.from_int(n, 0)
+    reg.apply_gates([O.hadamard(i) for i in range(n)] + [O.rz(0.3 * i, i) for i in range(n)], fuse=1)
+    before = reg.state
+    reg.apply_gates(ops + inv, fuse=1)
+    assert value_equal(reg.state, before)

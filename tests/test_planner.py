@@ -1,0 +1,80 @@
+"""CPU checks of the tile planner (quaru_gb300/csrc/qs_plan.cpp) with an emulated tile kernel.
+
+tests/cpp/tile_emulator.cpp links the engine's own planner and classifier
+and replays the planned stages tile by tile on the CPU; the result must equal
+the oracle's gate-by-gate amplitudes (value-exact: the emulator applies each
+gate with the oracle's arithmetic for k <= 2).
+"""
+from __future__ import annotations
+
+import struct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+SRC = ROOT / "tests" / "cpp" / "tile_emulator.cpp"
+EXE = ROOT / "tests" / "cpp" / "_build" / "tile_emulator"
+
+
+@pytest.fixture(scope="module")
+def emulator():
+    EXE.parent.mkdir(exist_ok=True)
+    srcs = [SRC, ROOT / "quaru_gb300/csrc/qs_plan.cpp", ROOT / "quaru_gb300/csrc/qs_classify.cpp"]
+    if not EXE.exists() or EXE.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
+        import shutil
+
+        nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+        cuda_inc = Path(nvcc).resolve().parent.parent / "include"
+        subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-I", str(ROOT / "include"),
+                        "-I", str(cuda_inc), *map(str, srcs), "-o", str(EXE)], check=True)
+    return EXE
+
+
+def run_emulator(exe, n, T, L, ops, state):
+    buf = bytearray(struct.pack("<4i", n, T, L, len(ops)))
+    for op in ops:
+        t = list(op.targets)
+        buf += struct.pack("<i", len(t)) + struct.pack(f"<{len(t)}i", *t)
+        buf += np.ascontiguousarray(np.asarray(op.matrix, dtype=np.complex128)).tobytes()
+    buf += np.ascontiguousarray(state, dtype=np.complex128).tobytes()
+    r = subprocess.run([str(exe)], input=bytes(buf), capture_output=True, check=True)
+    out = np.frombuffer(r.stdout[: 16 << n], dtype=np.complex128)
+    stages = struct.unpack("<i", r.stdout[16 << n:])[0]
+    return out, stages
+
+
+def cases():
+    from quaru_gb300 import operation as O
+    from quaru_gb300.operation import Operation
+    from quaru_gb300.workloads import SplitMix64, config1_circuit, flatten, layered_circuit, random_gate
+
+    c = config1_circuit()
+    yield "config1", c.n, c.gates
+    yield "layered14", 14, flatten(layered_circuit(14, 6, 3))
+    rng = np.random.default_rng(3)
+    sm = SplitMix64(11)
+    ops = [random_gate(sm, 13) for _ in range(250)]
+    for _ in range(10):
+        a, b, cc, d, e = (int(x) for x in rng.permutation(13)[:5])
+        ops.insert(int(rng.integers(len(ops))), O.to_controlled(Operation(np.array([[0.6, 0.8], [0.8, -0.6]]), [a]), b))
+        ops.insert(int(rng.integers(len(ops))), O.cnz([b, cc, d], a))
+        ops.insert(int(rng.integers(len(ops))), O.cnx([a, b, cc, d], e))
+    yield "controls", 13, ops
+
+
+@pytest.mark.parametrize("T,L", [(11, 5), (8, 3), (6, 6), (12, 5)])
+def test_planned_tiles_match_oracle(emulator, oracle_mod, T, L):
+    for name, n, ops in cases():
+        rng = np.random.default_rng(len(ops))
+        st = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        st /= np.linalg.norm(st)
+        o = oracle_mod.OracleRegister.from_int(n, 0)
+        o.state = st.copy()
+        o.apply_sequence([(g.matrix, g.targets) for g in ops])
+        got, stages = run_emulator(emulator, n, min(T, n), min(L, n), ops, st)
+        assert stages < len(ops), name
+        bad = np.nonzero(~((got.view(np.float64) == o.state.view(np.float64))))[0]
+        assert bad.size == 0, f"{name}: {bad.size} values differ, first at {bad[:4]}"
