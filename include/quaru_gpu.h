@@ -159,6 +159,52 @@ int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, dou
 int qs_measure_probabilities_noalloc(const void* state, size_t n, int precision, size_t target,
                                      double* out, void* stream, size_t* err);
 
+/* ---- observables and gradients (no counterpart in the reference) ---------- */
+
+/* <a|b> = sum_i conj(a_i) b_i accumulated in FP64 on the GPU; a and b may
+ * have different precisions (the fidelity of a complex64 run against a
+ * complex128 run is |<a|b>|^2). */
+int qs_inner_product(const qs_register* a, const qs_register* b, double* re, double* im);
+
+/* One term coeff * P of a Pauli-sum observable. P acts with X on the qubits
+ * in x_mask only, Z on z_mask only and Y on both (Y = iXZ per qubit). */
+typedef struct qs_pauli_term {
+    double coeff;
+    uint64_t x_mask;
+    uint64_t z_mask;
+} qs_pauli_term;
+
+/* <psi|H|psi> for H = sum_t coeff_t P_t, in FP64 on the GPU. */
+int qs_expval_pauli(qs_register* reg, const qs_pauli_term* terms, size_t nterms, double* value);
+
+/* Gates of a parameterised circuit. Rotations R_A(theta) = exp(-i theta A / 2)
+ * for A = X, Y, Z act on targets[0] with theta = params[param]; QS_GATE_FIXED
+ * is a matrix gate (k, targets, matrix as in qs_gate). */
+#define QS_GATE_FIXED 0
+#define QS_GATE_RX 1
+#define QS_GATE_RY 2
+#define QS_GATE_RZ 3
+typedef struct qs_param_gate {
+    int kind;
+    int param;
+    size_t k;
+    const size_t* targets;
+    const double* matrix;
+} qs_param_gate;
+
+/* Energy E = <psi|H|psi> of psi = U_m...U_1 |reg> and its gradient dE/dparams
+ * by the adjoint method: one forward pass, then a reverse pass that un-applies
+ * each gate from psi and from lambda = H psi and reads each rotation's
+ * derivative off Im<lambda|A|psi> (FP64 accumulation; FP32-pipe compensated
+ * sums on complex64 registers). No intermediate state is stored: memory is
+ * three state vectors. The register's state is the initial state and is
+ * unchanged on return. Gradients of rotations that share a parameter add up.
+ * Errors: InvalidTarget / InvalidDimensions as try_apply_fast with err[2] =
+ * gate index; QS_INVALID_ARGUMENT for a bad kind or parameter index. */
+int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, const double* params,
+                        size_t nparams, const qs_pauli_term* terms, size_t nterms, double* energy,
+                        double* grad, size_t* err);
+
 /* ---- host views ---------------------------------------------------------- */
 
 /* Read `pub state` (src/register.rs:35): 2^n complex, interleaved doubles. */

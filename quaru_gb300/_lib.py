@@ -48,6 +48,17 @@ class QsCircuitOptions(ctypes.Structure):
                 ("reserved", ctypes.c_int)]
 
 
+class QsPauliTerm(ctypes.Structure):
+    _fields_ = [("coeff", ctypes.c_double), ("x_mask", ctypes.c_uint64), ("z_mask", ctypes.c_uint64)]
+
+
+class QsParamGate(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("param", ctypes.c_int), ("k", ctypes.c_size_t), ("targets", _sp),
+                ("matrix", _dp)]
+
+
+QS_GATE_FIXED, QS_GATE_RX, QS_GATE_RY, QS_GATE_RZ = 0, 1, 2, 3
+
 SIGNATURES = {
     "qs_register_new": (_i, [_P(ctypes.c_uint8), _sz, _i, _P(_vp)]),
     "qs_register_from_int": (_i, [_sz, _sz, _i, _P(_vp)]),
@@ -63,6 +74,9 @@ SIGNATURES = {
     "qs_try_measure": (_i, [_vp, _sz, ctypes.c_double, _P(_i), _dp, _dp, _sp]),
     "qs_measure_probabilities": (_i, [_vp, _sz, _dp, _dp, _sp]),
     "qs_measure_probabilities_noalloc": (_i, [_vp, _sz, _i, _sz, _vp, _vp, _sp]),
+    "qs_inner_product": (_i, [_vp, _vp, _dp, _dp]),
+    "qs_expval_pauli": (_i, [_vp, _P(QsPauliTerm), _sz, _dp]),
+    "qs_adjoint_gradient": (_i, [_vp, _P(QsParamGate), _sz, _dp, _sz, _P(QsPauliTerm), _sz, _dp, _dp, _sp]),
     "qs_get_state": (_i, [_vp, _dp]),
     "qs_set_state": (_i, [_vp, _dp]),
     "qs_probabilities": (_i, [_vp, _dp]),

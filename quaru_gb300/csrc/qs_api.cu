@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "qs_adjoint.h"
 #include "qs_circuit.h"
 #include "qs_internal.h"
 #include "qs_kernels.h"
@@ -286,6 +287,39 @@ int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, dou
     if (prob0) *prob0 = reg->hres[0];
     if (prob1) *prob1 = reg->hres[1];
     return QS_OK;
+}
+
+int qs_inner_product(const qs_register* a, const qs_register* b, double* re, double* im) {
+    if (!a || !b) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (a->n != b->n) return set_err(QS_INVALID_ARGUMENT, "registers differ in size");
+    QS_CUDA(cudaStreamSynchronize(b->stream), "inner sync");
+    qs_register* ra = const_cast<qs_register*>(a);
+    if (qs::inner_product(a->state, a->prec, b->state, b->prec, a->n, ra->stream, ra->sms, ra->partials, ra->dres))
+        return cuda_fail(cudaGetLastError(), "inner product");
+    QS_CUDA(cudaMemcpyAsync(ra->hres, ra->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, ra->stream), "inner readback");
+    QS_CUDA(cudaStreamSynchronize(ra->stream), "inner sync");
+    if (re) *re = ra->hres[0];
+    if (im) *im = ra->hres[1];
+    return QS_OK;
+}
+
+int qs_expval_pauli(qs_register* reg, const qs_pauli_term* terms, size_t nterms, double* value) {
+    if (!reg || !value || (nterms && !terms)) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    std::string msg;
+    int rc = qs::expval_pauli(reg->state, reg->prec, reg->n, terms, nterms, reg->stream, reg->sms, value, &msg);
+    return rc ? set_err(rc, msg) : QS_OK;
+}
+
+int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, const double* params, size_t nparams,
+                        const qs_pauli_term* terms, size_t nterms, double* energy, double* grad, size_t* err) {
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if ((m && !gates) || (nparams && !params) || (nterms && !terms))
+        return set_err(QS_INVALID_ARGUMENT, "null argument");
+    if (reg->n < 1) return set_err(QS_INVALID_ARGUMENT, "register has no qubits");
+    std::string msg;
+    int rc = qs::adjoint_gradient(reg->state, reg->n, reg->prec, reg->arith, gates, m, params, nparams, terms, nterms,
+                                  reg->stream, reg->sms, energy, grad, err, &msg);
+    return rc ? set_err(rc, msg) : QS_OK;
 }
 
 uint64_t qs_launch_count(void) { return qs::g_launches.load(std::memory_order_relaxed); }

@@ -253,3 +253,91 @@ class Register:
 
     def synchronize(self) -> None:
         _check(_lib.load().qs_synchronize(self._h))
+
+    # ---- observables and gradients
+    def inner_product(self, other: "Register") -> complex:
+        """<self|other> accumulated in FP64 on the GPU."""
+        re, im = ctypes.c_double(0), ctypes.c_double(0)
+        _check(_lib.load().qs_inner_product(self._h, other._h, ctypes.byref(re), ctypes.byref(im)))
+        return complex(re.value, im.value)
+
+    def expval_pauli(self, terms) -> float:
+        """<psi|H|psi> for H = sum of (coeff, x_mask, z_mask) Pauli terms."""
+        arr = _pauli_array(terms)
+        v = ctypes.c_double(0)
+        _check(_lib.load().qs_expval_pauli(self._h, arr, len(terms), ctypes.byref(v)))
+        return v.value
+
+    def adjoint_gradient(self, gates, params, terms):
+        """Energy and gradient of the parameterised circuit `gates` (see ParamGate) for observable `terms`."""
+        n = len(gates)
+        cg = (_lib.QsParamGate * max(1, n))()
+        keep = []
+        for i, g in enumerate(gates):
+            cg[i].kind = g.kind
+            cg[i].param = g.param
+            if g.kind == _lib.QS_GATE_FIXED:
+                m = _matrix(g.op.matrix)
+                t = np.ascontiguousarray(np.array(list(g.op.targets), dtype=np.uintp))
+                cg[i].k = len(t)
+                cg[i].matrix = _dp(m.view(np.float64))
+            else:
+                m = None
+                t = np.ascontiguousarray(np.array([g.target], dtype=np.uintp))
+                cg[i].k = 1
+            cg[i].targets = _sp(t)
+            keep += [m, t]
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float64))
+        arr = _pauli_array(terms)
+        grad = np.zeros(max(1, p.size), dtype=np.float64)
+        e = ctypes.c_double(0)
+        err = np.zeros(3, dtype=np.uintp)
+        _check(_lib.load().qs_adjoint_gradient(self._h, cg, n, _dp(p), p.size, arr, len(terms), ctypes.byref(e),
+                                               _dp(grad), _sp(err)), err)
+        return e.value, grad[: p.size]
+
+
+class ParamGate:
+    """A gate of a parameterised circuit: a rotation R_A(params[param]) on `target`, or a fixed Operation."""
+
+    def __init__(self, kind: int, target: int = 0, param: int = -1, op: Operation | None = None):
+        self.kind, self.target, self.param, self.op = kind, target, param, op
+
+    @classmethod
+    def rx(cls, target: int, param: int) -> "ParamGate":
+        return cls(_lib.QS_GATE_RX, target, param)
+
+    @classmethod
+    def ry(cls, target: int, param: int) -> "ParamGate":
+        return cls(_lib.QS_GATE_RY, target, param)
+
+    @classmethod
+    def rz(cls, target: int, param: int) -> "ParamGate":
+        return cls(_lib.QS_GATE_RZ, target, param)
+
+    @classmethod
+    def fixed(cls, op: Operation) -> "ParamGate":
+        return cls(_lib.QS_GATE_FIXED, op=op)
+
+    def operation(self, params) -> Operation:
+        """The gate as a plain Operation at the given parameters."""
+        from . import operation as O
+
+        if self.kind == _lib.QS_GATE_FIXED:
+            return self.op
+        th = float(params[self.param])
+        if self.kind == _lib.QS_GATE_RY:
+            return O.ry(th, self.target)
+        if self.kind == _lib.QS_GATE_RZ:
+            return O.rz(th, self.target)
+        c, s = np.cos(th / 2.0), np.sin(th / 2.0)
+        return Operation(np.array([[c, -1j * s], [-1j * s, c]], dtype=np.complex128), [self.target])
+
+
+def _pauli_array(terms):
+    arr = (_lib.QsPauliTerm * max(1, len(terms)))()
+    for i, (c, x, z) in enumerate(terms):
+        arr[i].coeff = float(c)
+        arr[i].x_mask = int(x)
+        arr[i].z_mask = int(z)
+    return arr

@@ -133,3 +133,37 @@ def layered_circuit(n: int, depth: int, seed: int) -> list[list[Operation]]:
 
 def flatten(layers: list[list[Operation]]) -> list[Operation]:
     return [g for layer in layers for g in layer]
+
+
+# ---------------------------------------------------------------- configuration 4 (and 5)
+def ansatz(n: int, layers: int):
+    """Hardware-efficient ansatz: per layer RY(theta) then RZ(theta) on every qubit, then a CNOT
+    ladder i -> i+1 for i = 0..n-2. Returns (ParamGate list, number of parameters)."""
+    from .register import ParamGate
+
+    gates = []
+    p = 0
+    for _ in range(layers):
+        for q in range(n):
+            gates.append(ParamGate.ry(q, p))
+            p += 1
+        for q in range(n):
+            gates.append(ParamGate.rz(q, p))
+            p += 1
+        for q in range(n - 1):
+            gates.append(ParamGate.fixed(O.cnot(q, q + 1)))
+    return gates, p
+
+
+def chain_hamiltonian(n: int, rng: SplitMix64):
+    """sum_{i<n-1} a_i Z_i Z_{i+1} + sum_i b_i X_i with a, b ~ N(0, 1): (coeff, x_mask, z_mask) terms."""
+    terms = [(rng.normal(), 0, (1 << i) | (1 << (i + 1))) for i in range(n - 1)]
+    terms += [(rng.normal(), 1 << i, 0) for i in range(n)]
+    return terms
+
+
+def config4(n: int = 20, layers: int = 10, seed: int | None = None):
+    rng = SplitMix64(seed_for(4) if seed is None else seed)
+    gates, npar = ansatz(n, layers)
+    params = [2.0 * math.pi * rng.uniform() for _ in range(npar)]
+    return gates, params, chain_hamiltonian(n, rng)
