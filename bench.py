@@ -65,11 +65,12 @@ def read_peaks() -> tuple[float, str]:
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def read_traffic() -> float | None:
+def read_traffic(precision: str, arith: str) -> float | None:
+    """DRAM bytes per launch of the dense 1-qubit kernel at 30 qubits, from the committed ncu summary."""
     p = ROOT / "profiles" / "roofline_traffic.json"
     if p.exists():
         try:
-            return float(json.loads(p.read_text())["dense1_c128_30q_bytes_per_launch"])
+            return float(json.loads(p.read_text())[f"dense1_{precision}_{arith}_30q_bytes_per_launch"])
         except Exception:
             return None
     return None
@@ -267,7 +268,7 @@ def run_ours(args) -> None:
     clk = clocks.summary()
 
     fused = None
-    if args.fused:
+    if not args.no_fused:
         # The same layers through qs_apply_circuit with cache-blocked stages.
         fl = [g for i in range(args.warmup, args.warmup + args.steps) for g in layer(i)]
         reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=1)
@@ -282,6 +283,8 @@ def run_ours(args) -> None:
         fs = f0.elapsed_time(f1) / 1e3
         fused = {"gates_per_s": len(fl) / fs, "ms_per_step": 1e3 * fs / args.steps,
                  "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0)}
+
+    adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
 
     t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
     if dist:
@@ -326,21 +329,57 @@ def run_ours(args) -> None:
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": 16},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "k_dense1 (dense 1-qubit gate sweep)", "bound": "hbm", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": read_traffic(),
-                     "peak_source": peak_kind,
-                     "fp64_pipe": {"achieved_tflops": flops_per_launch / avg_haar_s / 1e12,
-                                   "peak_tflops": FP64_PEAK_TFLOPS_MEASURED,
-                                   "frac": flops_per_launch / avg_haar_s / 1e12 / FP64_PEAK_TFLOPS_MEASURED}},
+        "roofline": {"kernel": f"k_dense1 (dense 1-qubit gate sweep, {args.precision}, {args.arith} arithmetic)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": read_traffic(args.precision, args.arith), "peak_source": peak_kind,
+                     "bytes_per_launch": per_launch_bytes,
+                     "fp64_equivalent_tflops": flops_per_launch / avg_haar_s / 1e12,
+                     "fp64_pipe_peak_tflops_measured": FP64_PEAK_TFLOPS_MEASURED},
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
         "clocks": clk,
         "fused": fused,
+        "adjoint": adjoint,
         "cpu_baseline": cpu,
         "probe": {"p0_qubit0": p0},
     }
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def adjoint_section(q, torch, args) -> dict:
+    """Gradient throughput on the 20-qubit, 10-layer ansatz (400 parameters, ZZ + X chain observable):
+    FP64 (complex128) vs mixed (complex64 state, FP64-accurate accumulations), and the mixed run's 1 - F."""
+    from quaru_gb300.workloads import config4
+
+    gates, params, terms = config4()
+    n = 20
+    out = {"workload": "20-qubit hardware-efficient ansatz, 10 layers (RY, RZ on every qubit + CNOT ladder), "
+                       "400 parameters, H = sum a_i Z_i Z_i+1 + sum b_i X_i"}
+    grads = {}
+    for name, prec in (("fp64", q.QS_PREC_C128), ("mixed", q.QS_PREC_C64)):
+        reg = q.Register.from_int(n, 0, precision=prec)
+        reg.set_arith(q.QS_ARITH_FMA)
+        for _ in range(3):
+            e, g = reg.adjoint_gradient(gates, params, terms)
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e, g = reg.adjoint_gradient(gates, params, terms)
+        dt = (time.perf_counter() - t0) / reps
+        grads[name] = g
+        out[name] = {"ms_per_gradient": 1e3 * dt, "grads_per_s": len(params) / dt, "energy": e}
+    out["mixed_vs_fp64_speedup"] = out["fp64"]["ms_per_gradient"] / out["mixed"]["ms_per_gradient"]
+    out["max_grad_diff_mixed_vs_fp64"] = float(np.max(np.abs(grads["mixed"] - grads["fp64"])))
+    a = q.Register.from_int(n, 0)
+    a.set_arith(q.QS_ARITH_FMA)
+    b = q.Register.from_int(n, 0, precision=q.QS_PREC_C64)
+    ops = [gt.operation(params) for gt in gates]
+    a.apply_gates(ops)
+    b.apply_gates(ops)
+    f = abs(b.inner_product(a)) ** 2 / (a.inner_product(a).real * b.inner_product(b).real)
+    out["mixed_one_minus_fidelity"] = 1.0 - f
+    return out
 
 
 def _measure_probs(lib, reg, target: int) -> float:
@@ -361,12 +400,13 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
-    ap.add_argument("--arith", choices=["exact", "fma", "df64"], default="fma")
+    ap.add_argument("--arith", choices=["exact", "fma", "df64"], default="df64")
     ap.add_argument("--cpu-qubits", type=int, default=24)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-qubits", type=int, default=26)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--fused", action="store_true", help="also time the fused (tiled) circuit path")
+    ap.add_argument("--no-fused", action="store_true", help="skip the fused (tiled) circuit timing")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")
