@@ -283,6 +283,20 @@ def run_ours(args) -> None:
         fs = f0.elapsed_time(f1) / 1e3
         fused = {"gates_per_s": len(fl) / fs, "ms_per_step": 1e3 * fs / args.steps,
                  "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0)}
+        if prec == q.QS_PREC_C64:
+            # dense 5-qubit blocks as 3xTF32 tensor-core GEMMs
+            b0 = torch.cuda.Event(enable_timing=True)
+            b1 = torch.cuda.Event(enable_timing=True)
+            reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=2)
+            barrier()
+            l0 = lib.qs_launch_count()
+            b0.record(stream)
+            reg.apply_gates(fl, fuse=2)
+            b1.record(stream)
+            barrier()
+            bs = b0.elapsed_time(b1) / 1e3
+            fused["blocks_tf32x3"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
+                                      "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0)}
 
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
 

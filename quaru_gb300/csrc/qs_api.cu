@@ -242,7 +242,7 @@ int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m, const qs_
         }
         qs::classify_gate(gates[g].matrix, gates[g].k, gates[g].targets, &ops[g]);
     }
-    int rc = qs::run_circuit(reg->state, reg->n, reg->prec, reg->arith, ops, o, reg->stream, reg->sms, &msg);
+    int rc = qs::run_circuit(reg->state, reg->n, reg->prec, reg->arith, ops, gates, o, reg->stream, reg->sms, &msg);
     return rc ? set_err(rc, msg) : QS_OK;
 }
 

@@ -8,6 +8,7 @@
 
 #include "qs_circuit.h"
 #include "qs_kernels.h"
+#include "qs_fuse.h"
 #include "qs_tile.h"
 
 namespace qs {
@@ -64,8 +65,50 @@ int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStre
     return e == cudaSuccess ? QS_OK : fail(e, "wide gate", msg);
 }
 
-int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
+// fuse == 2: dense blocks of up to max_width qubits. On complex64 registers of
+// at least 12 qubits the blocks run as 3xTF32 tensor-core GEMMs inside
+// 12-qubit tiles; otherwise each block is one dense gate sweep.
+static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* gates, size_t m,
+                      const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
+    const int W = std::max(2, std::min(5, opts.max_width > 0 ? opts.max_width : 5));
+    std::vector<FusedBlock> blocks = fuse_blocks(gates, m, W);
+    const bool tensor = (prec == QS_PREC_C64) && n >= 12;
+    std::vector<OpDesc> ops;
+    std::vector<float> frags;
+    for (FusedBlock& b : blocks) {
+        std::vector<size_t> tq(b.qubits.begin(), b.qubits.end());
+        OpDesc op;
+        if (tensor && int(b.qubits.size()) <= 5) {
+            pad_block(&b, 5, n);
+            op.kind = OP_BLOCK;
+            op.k = 5;
+            op.orig_k = 5;
+            for (int j = 0; j < 5; j++) op.tq[j] = b.qubits[j];
+            op.touched_rows = 32;
+            op.block = int(frags.size() / (4 * kBlockFragFloat4));
+            frags.resize(frags.size() + 4 * kBlockFragFloat4);
+            block_fragments(b.u, frags.data() + frags.size() - 4 * kBlockFragFloat4);
+        } else {
+            tq.assign(b.qubits.begin(), b.qubits.end());
+            classify_gate(b.u.data(), tq.size(), tq.data(), &op);
+        }
+        ops.push_back(std::move(op));
+    }
+    if (!tensor) {
+        for (const OpDesc& op : ops) {
+            int rc = apply_op(state, n, prec, arith, op, s, sms, msg);
+            if (rc) return rc;
+        }
+        return QS_OK;
+    }
+    const int T = std::min(12, n), L = std::min(5, T);
+    std::vector<TileStage> stages = plan_tiles(ops, n, T, L, false);
+    return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg, &frags);
+}
+
+int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops, const qs_gate* gates,
                 const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
+    if (opts.fuse == 2 && gates) return run_blocks(state, n, prec, arith, gates, ops.size(), opts, s, sms, msg);
     if (opts.fuse >= 1) {
         // Tile qubits: 32 KiB of shared memory per tile by default.
         int T = opts.tile_qubits > 0 ? opts.tile_qubits : (prec == QS_PREC_C64 ? 12 : 11);

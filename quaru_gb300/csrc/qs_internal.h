@@ -26,6 +26,7 @@ enum OpKind : int {
     OP_DENSE_REAL = 2,  // dense sub-matrix whose imaginary parts are all zero
     OP_MONO = 3,        // one non-zero per row/column, general complex phases
     OP_MONO_PF = 4,     // one non-zero per row/column, every value in {1, -1, i, -i}
+    OP_BLOCK = 11,      // fused dense 5-qubit block (tensor-core tiles)
 };
 
 // Phase classes of OP_MONO_PF rows (value-exact moves, no arithmetic).
@@ -48,6 +49,7 @@ struct OpDesc {
     std::vector<double> phase;    // monomial: complex factor of each row
     std::vector<uint8_t> pf;      // monomial: PfClass per row (PF_SKIP for untouched rows)
     uint64_t touched_rows = 0;    // number of sub-rows the gate rewrites (for byte accounting)
+    int block = -1;               // OP_BLOCK: index of the fused block
 };
 
 // Shape/target validation in the order of Register::try_apply_fast

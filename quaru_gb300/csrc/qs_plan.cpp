@@ -20,6 +20,7 @@ namespace qs {
 
 bool tileable(const OpDesc& op) {
     if (op.kind == OP_NOOP) return true;
+    if (op.kind == OP_BLOCK) return op.k == 5;
     if (op.k + __builtin_popcountll(op.fixmask) > 16) return false;
     if (op.kind == OP_DENSE || op.kind == OP_DENSE_REAL) return op.k == 1;
     return op.k <= 3;  // monomial
@@ -133,14 +134,16 @@ TileOp make_tile_op(const OpDesc& op, const TileStage& st) {
             lo = hi + 1;
         }
     }
-    const int D = 1 << op.k;
+    const int D = (op.kind == OP_BLOCK) ? 0 : (1 << op.k);
     for (int r = 0; r < D; r++) {
         uint32_t o = 0;
         for (int b = 0; b < op.k; b++)
             if (r >> b & 1) o |= 1u << t.tb[b];
         t.off[r] = o;
     }
-    if (op.kind == OP_MONO || op.kind == OP_MONO_PF) {
+    if (op.kind == OP_BLOCK) {
+        t.bidx = uint32_t(op.block) * kBlockFragFloat4;
+    } else if (op.kind == OP_MONO || op.kind == OP_MONO_PF) {
         for (int r = 0; r < D; r++) {
             t.offsrc[r] = t.off[op.perm[r]];
             t.pf[r] = op.pf[r];
@@ -166,6 +169,127 @@ TileOp make_tile_op(const OpDesc& op, const TileStage& st) {
     }
     for (int i = 0; i < 16; i++) t.mf[i] = float(t.m[i]);
     return t;
+}
+
+// cvt.rna.tf32.f32 on the host: round to nearest (ties away) at 10 fraction bits.
+static float tf32_rna(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b = (b + 0x1000u) & ~0x1FFFu;
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+}
+
+void block_fragments(const std::vector<double>& u, float* out) {
+    auto M = [&](int n, int k) -> double {  // [[Ur, -Ui], [Ui, Ur]]
+        const int r = n & 31, c = k & 31;
+        const double re = u[2 * (r * 32 + c)], im = u[2 * (r * 32 + c) + 1];
+        if ((n < 32) == (k < 32)) return re;
+        return (n < 32) ? -im : im;
+    };
+    for (int nt = 0; nt < 8; nt++)
+        for (int ks = 0; ks < 8; ks++)
+            for (int lane = 0; lane < 32; lane++) {
+                const int g = lane >> 2, t = lane & 3;
+                const double v0 = M(8 * nt + g, 8 * ks + t), v1 = M(8 * nt + g, 8 * ks + t + 4);
+                const float h0 = tf32_rna(float(v0)), h1 = tf32_rna(float(v1));
+                float* o = out + 4 * ((nt * 8 + ks) * 32 + lane);
+                o[0] = h0;
+                o[1] = h1;
+                o[2] = tf32_rna(float(v0 - double(h0)));
+                o[3] = tf32_rna(float(v1 - double(h1)));
+            }
+}
+
+// Whether a tile op can join a register group (k <= 1 dense or monomial).
+static bool groupable(const TileOp& t) {
+    if (t.kind == OP_DENSE || t.kind == OP_DENSE_REAL) return t.k == 1;
+    if (t.kind == OP_MONO || t.kind == OP_MONO_PF) return t.k <= 1;
+    return false;
+}
+
+static TileOp group_header(uint32_t gbits, int T, int count) {
+    TileOp h;
+    std::memset(&h, 0, sizeof(h));
+    h.kind = OP_GROUP;
+    h.k = uint8_t(count);
+    std::vector<int> pos;
+    for (int b = 0; b < T; b++)
+        if (gbits >> b & 1u) pos.push_back(b);
+    h.npos = uint8_t(pos.size());
+    for (size_t i = 0; i < pos.size(); i++) h.pos[i] = uint8_t(pos[i]);
+    int lo = 0;
+    for (size_t j = 0; j <= pos.size(); j++) {
+        const int hi = (j < pos.size()) ? pos[j] : 32;
+        uint32_t m = 0;
+        for (int b = lo; b < hi && b < 32; b++) m |= 1u << b;
+        h.seg[j] = m;
+        lo = hi + 1;
+    }
+    for (int j = 0; j < (1 << kGroupBits); j++) {
+        uint32_t o = 0;
+        for (int b = 0; b < kGroupBits; b++)
+            if (j >> b & 1) o |= 1u << pos[b];
+        h.off[j] = o;
+    }
+    return h;
+}
+
+std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& st, bool groups) {
+    std::vector<TileOp> prog, members;
+    uint32_t gbits = 0;
+    auto flush = [&]() {
+        if (members.size() >= 2) {
+            // pad the group to exactly kGroupBits tile bits
+            for (int b = 0; b < st.T && __builtin_popcount(gbits) < kGroupBits; b++) gbits |= 1u << b;
+            std::vector<int> pos;
+            for (int b = 0; b < st.T; b++)
+                if (gbits >> b & 1u) pos.push_back(b);
+            auto gl = [&](int lb) -> int {
+                for (size_t i = 0; i < pos.size(); i++)
+                    if (pos[i] == lb) return int(i);
+                return -1;
+            };
+            prog.push_back(group_header(gbits, st.T, int(members.size())));
+            for (TileOp m : members) {
+                m.gj = (m.k == 1) ? uint8_t(gl(m.tb[0])) : 0;
+                // local fixed bits: positions other than the target, with values in lfixval
+                for (int i = 0; i < m.npos; i++) {
+                    const int lb = m.pos[i];
+                    if (m.k == 1 && lb == m.tb[0]) continue;
+                    const bool one = (m.lfixval >> lb) & 1u;
+                    const int j = gl(lb);
+                    if (j >= 0) {
+                        m.gfin_mask |= uint8_t(1u << j);
+                        if (one) m.gfin_val |= uint8_t(1u << j);
+                    } else {
+                        m.gfout_mask |= 1u << lb;
+                        if (one) m.gfout_val |= 1u << lb;
+                    }
+                }
+                prog.push_back(m);
+            }
+        } else {
+            for (const TileOp& m : members) prog.push_back(m);
+        }
+        members.clear();
+        gbits = 0;
+    };
+    for (int idx : st.ops) {
+        TileOp t = make_tile_op(ops[idx], st);
+        if (groups && st.T >= kGroupBits && groupable(t)) {
+            const uint32_t need = (t.k == 1) ? (1u << t.tb[0]) : 0u;
+            if (__builtin_popcount(gbits | need) > kGroupBits) flush();
+            gbits |= need;
+            members.push_back(t);
+        } else {
+            flush();
+            prog.push_back(t);
+        }
+    }
+    flush();
+    return prog;
 }
 
 }  // namespace qs

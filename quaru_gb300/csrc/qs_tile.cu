@@ -256,10 +256,144 @@ __device__ __forceinline__ void dense_pair(const DenseCoef<2>& c, bool real, flo
     b = make_float4(oh[2], ol[2], oh[3], ol[3]);
 }
 
+// ---- register groups: the 8 amplitudes of a 3-bit sub-cube held in registers
 template <int REP>
-__global__ void __launch_bounds__(kTileThreads) k_tile(void* __restrict__ state, uint64_t ntiles,
+__device__ __forceinline__ typename TileElem<REP>::T mono_row(const TileOp& m, int r, typename TileElem<REP>::T src) {
+    const uint8_t c = m.pf[r];
+    if (c == 255) return phase_mul(m.m + 2 * r, src, REP);
+    return pf_move(src, c);
+}
+
+// Pair (a, b) of a k = 1 gate on group-local bit j; a has bit j clear.
+template <int REP>
+__device__ __forceinline__ void group_pair(const TileOp& m, const DenseCoef<REP>& c, bool dense, bool real,
+                                           typename TileElem<REP>::T& xa, typename TileElem<REP>::T& xb) {
+    using E = typename TileElem<REP>::T;
+    if (dense) {
+        dense_pair(c, real, xa, xb);
+    } else {
+        const E s0 = m.offsrc[0] ? xb : xa;
+        const E s1 = m.offsrc[1] ? xb : xa;
+        if (m.pf[0] != PF_SKIP_DEV) xa = mono_row<REP>(m, 0, s0);
+        if (m.pf[1] != PF_SKIP_DEV) xb = mono_row<REP>(m, 1, s1);
+    }
+}
+
+#define QS_GPAIR(A, B)                                                          \
+    if (((A) & fm) == fv) group_pair<REP>(m, c, dense, real, x[A], x[B]);
+
+template <int REP>
+__device__ __forceinline__ void group_apply(const TileOp& m, typename TileElem<REP>::T (&x)[8]) {
+    const int fm = m.gfin_mask, fv = m.gfin_val;
+    const int kind = m.kind;
+    if (m.k == 0) {  // phase or sign on the fixed subspace
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+            if ((r & fm) == fv && m.pf[0] != PF_SKIP_DEV) x[r] = mono_row<REP>(m, 0, x[r]);
+        return;
+    }
+    const bool dense = kind == OP_DENSE || kind == OP_DENSE_REAL;
+    const bool real = kind == OP_DENSE_REAL;
+    DenseCoef<REP> c;
+    if (dense) load_coef(c, m);
+    switch (m.gj) {
+        case 0:
+            QS_GPAIR(0, 1) QS_GPAIR(2, 3) QS_GPAIR(4, 5) QS_GPAIR(6, 7) break;
+        case 1:
+            QS_GPAIR(0, 2) QS_GPAIR(1, 3) QS_GPAIR(4, 6) QS_GPAIR(5, 7) break;
+        default:
+            QS_GPAIR(0, 4) QS_GPAIR(1, 5) QS_GPAIR(2, 6) QS_GPAIR(3, 7) break;
+    }
+}
+#undef QS_GPAIR
+
+// ---- fused 5-qubit blocks on the tensor cores (complex64 tiles, 3xTF32)
+__device__ __forceinline__ uint32_t f2tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t deposit5(uint32_t r, const uint8_t* pos) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int b = 0; b < 5; b++) o |= ((r >> b) & 1u) << pos[b];
+    return o;
+}
+
+// Y = U X for the 32-row block view of the tile: X^T (columns x 64 real) times
+// B = M^T, M = [[Ur, -Ui], [Ui, Ur]]; D = A_lo B_hi + A_hi B_lo + A_hi B_hi in FP32.
+// Warp w owns m-tiles w, w + 8, ... (16 columns each) and updates them in place.
+__device__ __forceinline__ void block_apply(float* sf, uint32_t tsize, const TileOp& op,
+                                            const float4* __restrict__ bfrag) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const uint32_t nmt = (tsize >> 5) >> 4;
+    uint8_t pos[5];
+#pragma unroll
+    for (int b = 0; b < 5; b++) pos[b] = op.pos[b];
+    uint32_t rd[8], wr[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) rd[j] = deposit5(uint32_t(4 * j + t), pos);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        wr[2 * q] = deposit5(uint32_t(8 * q + 2 * t), pos);
+        wr[2 * q + 1] = deposit5(uint32_t(8 * q + 2 * t + 1), pos);
+    }
+    const float4* bf = bfrag + op.bidx + lane;
+    for (uint32_t mt = warp; mt < nmt; mt += kTileThreads / 32) {
+        const uint32_t c0 = expand_local(16 * mt + g, pos, 5);
+        const uint32_t c1 = expand_local(16 * mt + g + 8, pos, 5);
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll 1
+        for (int comp = 0; comp < 2; comp++) {  // k-steps 0..3 read real parts, 4..7 imaginary parts
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int ks = 4 * comp + q;
+                const float a0 = sf[2 * (c0 | rd[2 * q]) + comp], a1 = sf[2 * (c1 | rd[2 * q]) + comp];
+                const float a2 = sf[2 * (c0 | rd[2 * q + 1]) + comp], a3 = sf[2 * (c1 | rd[2 * q + 1]) + comp];
+                const uint32_t h0 = f2tf32(a0), h1 = f2tf32(a1), h2 = f2tf32(a2), h3 = f2tf32(a3);
+                const uint32_t l0 = f2tf32(a0 - __uint_as_float(h0)), l1 = f2tf32(a1 - __uint_as_float(h1));
+                const uint32_t l2 = f2tf32(a2 - __uint_as_float(h2)), l3 = f2tf32(a3 - __uint_as_float(h3));
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++) {
+                    const float4 b = __ldg(bf + (nt * 8 + ks) * 32);
+                    const uint32_t bh0 = __float_as_uint(b.x), bh1 = __float_as_uint(b.y);
+                    const uint32_t bl0 = __float_as_uint(b.z), bl1 = __float_as_uint(b.w);
+                    mma_tf32(acc[nt], l0, l1, l2, l3, bh0, bh1);
+                    mma_tf32(acc[nt], h0, h1, h2, h3, bl0, bl1);
+                    mma_tf32(acc[nt], h0, h1, h2, h3, bh0, bh1);
+                }
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            const int comp = nt >> 2, q = nt & 3;
+            sf[2 * (c0 | wr[2 * q]) + comp] = acc[nt][0];
+            sf[2 * (c0 | wr[2 * q + 1]) + comp] = acc[nt][1];
+            sf[2 * (c1 | wr[2 * q]) + comp] = acc[nt][2];
+            sf[2 * (c1 | wr[2 * q + 1]) + comp] = acc[nt][3];
+        }
+        __syncwarp();
+    }
+}
+
+template <int REP, bool BLK>
+__global__ void __launch_bounds__(kTileThreads, (REP == 3 && !BLK) ? 3 : 2) k_tile(void* __restrict__ state, uint64_t ntiles,
                                                        const __grid_constant__ StageArgs sa,
-                                                       const TileOp* __restrict__ ops) {
+                                                       const TileOp* __restrict__ ops,
+                                                       const float4* __restrict__ bfrag) {
     using E = typename TileElem<REP>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     E* s = reinterpret_cast<E*>(smem_raw);
@@ -297,7 +431,32 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(void* __restrict__ state,
 #pragma unroll
             for (int j = 0; j < 5; j++) seg[j] = op.seg[j];
             const int kind = op.kind;
-            if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
+            if (BLK) {
+                if constexpr (REP == 3 && BLK)
+                    if (kind == OP_BLOCK) block_apply(reinterpret_cast<float*>(s), tsize, op, bfrag);
+            } else if (REP == 3 && kind == OP_GROUP) {
+              if constexpr (REP == 3 && !BLK) {
+                const int cnt = op.k;
+                uint32_t goff[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) goff[j] = op.off[j];
+                for (uint32_t p = threadIdx.x; p < ntup; p += kTileThreads) {
+                    const uint32_t b0 = tuple_index(p, npos, seg, op.pos, 0u);
+                    E x[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) x[j] = s[b0 + goff[j]];
+                    for (int mi = 1; mi <= cnt; mi++) {
+                        const TileOp& m = sops[o + mi];
+                        if ((base & m.omask) != m.oval) continue;
+                        if ((b0 & m.gfout_mask) != m.gfout_val) continue;
+                        group_apply<REP>(m, x);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; j++) s[b0 + goff[j]] = x[j];
+                }
+                o += cnt;
+              }
+            } else if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
                 const uint32_t tb = op.off[1];
                 const bool real = kind == OP_DENSE_REAL;
                 DenseCoef<REP> c;
@@ -311,24 +470,16 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(void* __restrict__ state,
                 }
             } else if (kind == OP_MONO || kind == OP_MONO_PF) {
                 const int D = 1 << op.k;
-                uint32_t off[8], offsrc[8];
-                uint8_t pf[8];
-#pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    off[r] = op.off[r];
-                    offsrc[r] = op.offsrc[r];
-                    pf[r] = (r < D) ? op.pf[r] : uint8_t(PF_SKIP_DEV);
-                }
                 for (uint32_t p = threadIdx.x; p < ntup; p += kTileThreads) {
                     const uint32_t i0 = tuple_index(p, npos, seg, op.pos, fixv);
                     E y[8];
 #pragma unroll
                     for (int r = 0; r < 8; r++)
-                        if (pf[r] != PF_SKIP_DEV) y[r] = s[i0 + offsrc[r]];
+                        if (r < D && op.pf[r] != PF_SKIP_DEV) y[r] = s[i0 + op.offsrc[r]];
 #pragma unroll
                     for (int r = 0; r < 8; r++) {
-                        if (pf[r] == PF_SKIP_DEV) continue;
-                        s[i0 + off[r]] = (pf[r] == 255) ? phase_mul(op.m + 2 * r, y[r], REP) : pf_move(y[r], pf[r]);
+                        if (r >= D || op.pf[r] == PF_SKIP_DEV) continue;
+                        s[i0 + op.off[r]] = mono_row<REP>(op, r, y[r]);
                     }
                 }
             }
@@ -345,9 +496,9 @@ static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
     return e == cudaErrorMemoryAllocation ? QS_OUT_OF_MEMORY : QS_CUDA_ERROR;
 }
 
-template <int REP>
+template <int REP, bool BLK>
 static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_begin, int op_end,
-                               const TileOp* dops, cudaStream_t s, int sms) {
+                               const TileOp* dops, const float4* dfrag, cudaStream_t s, int sms) {
     using E = typename TileElem<REP>::T;
     StageArgs sa;
     std::memset(&sa, 0, sizeof(sa));
@@ -366,13 +517,13 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     for (int b = 0; b < sa.H; b++) sa.high[b] = uint8_t(st.high[b]);
     const size_t smem = (sizeof(E) << st.T) + (sizeof(uint64_t) << sa.H) + sizeof(TileOp) * size_t(op_end - op_begin);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_tile<REP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaError_t e = cudaFuncSetAttribute(k_tile<REP, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
     }
     const uint64_t ntiles = 1ull << (n - st.T);
     const int per_sm = std::max(1, std::min(8, int((220 * 1024) / smem)));
     const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * per_sm);
-    k_tile<REP><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops);
+    k_tile<REP, BLK><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, dfrag);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) note_launches(1);
     return e;
@@ -388,7 +539,8 @@ static bool df64_range_ok(const OpDesc& op) {
 }
 
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
-              const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg) {
+              const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg,
+              const std::vector<float>* block_frags) {
     int rep = (prec == QS_PREC_C64) ? 3 : (arith == QS_ARITH_EXACT ? 0 : (arith == QS_ARITH_FMA ? 1 : 2));
     if (rep == 2)
         for (const auto& op : ops)
@@ -398,7 +550,9 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
     for (size_t i = 0; i < stages.size(); i++) {
         first[i] = int(host.size());
         if (!stages[i].tiled) continue;
-        for (int idx : stages[i].ops) host.push_back(make_tile_op(ops[idx], stages[i]));
+        // Register groups pay off where shared-memory passes dominate (complex64); the
+        // FP64 and double-float tiles are arithmetic-bound and keep one pass per gate.
+        for (const TileOp& t : stage_program(ops, stages[i], rep == 3)) host.push_back(t);
     }
     TileOp* dops = nullptr;
     if (!host.empty()) {
@@ -410,6 +564,17 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
             return tile_fail(e, "tile op upload", msg);
         }
     }
+    float4* dfrag = nullptr;
+    if (block_frags && !block_frags->empty()) {
+        cudaError_t e = cudaMallocAsync((void**)&dfrag, block_frags->size() * sizeof(float), s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dfrag, block_frags->data(), block_frags->size() * sizeof(float),
+                                cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) {
+            if (dops) cudaFreeAsync(dops, s);
+            return tile_fail(e, "block fragments", msg);
+        }
+    }
     int rc = QS_OK;
     for (size_t i = 0; i < stages.size() && rc == QS_OK; i++) {
         const TileStage& st = stages[i];
@@ -417,17 +582,23 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
             rc = apply_op(state, n, prec, arith, ops[st.single], s, sms, msg);
             continue;
         }
-        const int b = first[i], e2 = b + int(st.ops.size());
+        const int b = first[i], e2 = (i + 1 < stages.size()) ? first[i + 1] : int(host.size());
         cudaError_t e;
         switch (rep) {
-            case 0: e = launch_tile<0>(state, n, st, b, e2, dops, s, sms); break;
-            case 1: e = launch_tile<1>(state, n, st, b, e2, dops, s, sms); break;
-            case 2: e = launch_tile<2>(state, n, st, b, e2, dops, s, sms); break;
-            default: e = launch_tile<3>(state, n, st, b, e2, dops, s, sms); break;
+            case 0: e = launch_tile<0, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
+            case 1: e = launch_tile<1, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
+            case 2: e = launch_tile<2, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
+            default:
+                if (dfrag)
+                    e = launch_tile<3, true>(state, n, st, b, e2, dops, dfrag, s, sms);
+                else
+                    e = launch_tile<3, false>(state, n, st, b, e2, dops, dfrag, s, sms);
+                break;
         }
         if (e != cudaSuccess) rc = tile_fail(e, "tile kernel", msg);
     }
     if (dops) cudaFreeAsync(dops, s);
+    if (dfrag) cudaFreeAsync(dfrag, s);
     return rc;
 }
 

@@ -17,6 +17,8 @@
 namespace qs {
 
 constexpr int kTileMaxHigh = 8;
+constexpr int kGroupBits = 3;          // register-group width: 8 amplitudes per thread
+constexpr uint8_t OP_GROUP = 10;       // TileOp kind of a register-group header
 
 // Gate as the tile kernel sees it (local bit numbering inside the tile).
 struct TileOp {
@@ -36,7 +38,21 @@ struct TileOp {
     float dfh[16];    // dense 1q double-float coefficients (see Dense1Args)
     float dfl[16];
     float mf[16];     // m rounded to float (complex64 registers)
+    // Register-group member fields (valid when the op follows an OP_GROUP header):
+    uint8_t gj;          // group-local target bit (0..2)
+    uint8_t gfin_mask;   // fixed bits inside the group (group-local)
+    uint8_t gfin_val;
+    uint8_t pad_;
+    uint32_t gfout_mask; // fixed bits inside the tile but outside the group (tile-local)
+    uint32_t gfout_val;
+    uint32_t bidx;       // OP_BLOCK: offset of the block's B fragments (float4 units)
+    uint32_t pad2_;
 };
+
+// Tensor-core fragments of one fused 5-qubit block: [n-tile 8][k-step 8][lane 32] float4
+// (b0_hi, b1_hi, b0_lo, b1_lo) of B = M^T, M = [[Ur, -Ui], [Ui, Ur]] (64 x 64 real).
+constexpr uint32_t kBlockFragFloat4 = 8 * 8 * 32;
+void block_fragments(const std::vector<double>& u32x32, float* out /* 4 * kBlockFragFloat4 floats */);
 
 struct TileStage {
     bool tiled = false;
@@ -56,8 +72,14 @@ std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, 
 // Device image of one op inside `stage`.
 TileOp make_tile_op(const OpDesc& op, const TileStage& stage);
 
+// The device program of one stage: its ops, with runs of 1-qubit gates whose
+// targets span at most kGroupBits tile bits gathered behind OP_GROUP headers.
+// Gate order is unchanged.
+std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& stage, bool groups);
+
 // Run stages on the device; ops are the host descriptors.
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
-              const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg);
+              const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg,
+              const std::vector<float>* block_frags = nullptr);
 
 }  // namespace qs

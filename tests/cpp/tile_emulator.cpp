@@ -44,6 +44,36 @@ uint64_t expand(uint64_t t, const std::vector<int>& pos) {
     return t;
 }
 
+// One k <= 1 member op of a register group applied to the 8 registers x.
+void group_apply(const qs::TileOp& m, C (&x)[8]) {
+    const int fm = m.gfin_mask, fv = m.gfin_val;
+    auto mono_row = [&](int r, C src) -> C {
+        return (m.pf[r] == 255) ? cmul(m.m[2 * r], m.m[2 * r + 1], src) : pf(src, m.pf[r]);
+    };
+    if (m.k == 0) {
+        for (int r = 0; r < 8; r++)
+            if ((r & fm) == fv && m.pf[0] != 4) x[r] = mono_row(0, x[r]);
+        return;
+    }
+    const int j = m.gj;
+    for (int a = 0; a < 8; a++) {
+        if (a >> j & 1) continue;
+        if ((a & fm) != fv) continue;
+        const int b = a | (1 << j);
+        if (m.kind == qs::OP_DENSE || m.kind == qs::OP_DENSE_REAL) {
+            C y0 = cadd(cmul(m.m[0], m.m[1], x[a]), cmul(m.m[2], m.m[3], x[b]));
+            C y1 = cadd(cmul(m.m[4], m.m[5], x[a]), cmul(m.m[6], m.m[7], x[b]));
+            x[a] = y0;
+            x[b] = y1;
+        } else {
+            const C s0 = m.offsrc[0] ? x[b] : x[a];
+            const C s1 = m.offsrc[1] ? x[b] : x[a];
+            if (m.pf[0] != 4) x[a] = mono_row(0, s0);
+            if (m.pf[1] != 4) x[b] = mono_row(1, s1);
+        }
+    }
+}
+
 // Emulates k_tile<0> (the exact representation) for one stage.
 void run_stage(std::vector<C>& st, int n, const qs::TileStage& stage, const std::vector<qs::TileOp>& tops) {
     const int T = stage.T, L = stage.L, H = int(stage.high.size());
@@ -63,9 +93,27 @@ void run_stage(std::vector<C>& st, int n, const qs::TileStage& stage, const std:
     for (uint64_t tile = 0; tile < (1ull << (n - T)); tile++) {
         const uint64_t base = expand(tile, qpos);
         for (uint32_t i = 0; i < tsize; i++) s[i] = st[base + rowoff[i >> L] + (i & lmask)];
-        for (const qs::TileOp& op : tops) {
+        for (size_t oi = 0; oi < tops.size(); oi++) {
+            const qs::TileOp& op = tops[oi];
             if ((base & op.omask) != op.oval) continue;
             const uint32_t ntup = tsize >> op.npos;
+            if (op.kind == qs::OP_GROUP) {
+                for (uint32_t p = 0; p < ntup; p++) {
+                    uint32_t b0 = p & op.seg[0];
+                    for (int j = 1; j <= op.npos; j++) b0 |= (p << j) & op.seg[j];
+                    C x[8];
+                    for (int j = 0; j < 8; j++) x[j] = s[b0 + op.off[j]];
+                    for (int mi = 1; mi <= op.k; mi++) {
+                        const qs::TileOp& m = tops[oi + mi];
+                        if ((base & m.omask) != m.oval) continue;
+                        if ((b0 & m.gfout_mask) != m.gfout_val) continue;
+                        group_apply(m, x);
+                    }
+                    for (int j = 0; j < 8; j++) s[b0 + op.off[j]] = x[j];
+                }
+                oi += op.k;
+                continue;
+            }
             for (uint32_t p = 0; p < ntup; p++) {
                 uint32_t i0;
                 if (op.npos <= 4) {  // the kernel's segment-mask expansion
@@ -156,8 +204,7 @@ int main() {
             st.swap(out);
             continue;
         }
-        std::vector<qs::TileOp> tops;
-        for (int idx : stage.ops) tops.push_back(qs::make_tile_op(ops[idx], stage));
+        const std::vector<qs::TileOp> tops = qs::stage_program(ops, stage, true);
         run_stage(st, n, stage, tops);
     }
     fwrite(st.data(), sizeof(C), st.size(), stdout);

@@ -110,3 +110,36 @@ def test_fused_large_state_permutation_round_trip_bit_exact():
     before = reg.state
     reg.apply_gates(ops + inv, fuse=1)
     assert value_equal(reg.state, before)
+
+
+@pytest.mark.parametrize("n", [12, 14, 17])
+def test_dense_block_fusion_tensor_cores_c64(n):
+    """fuse=2 on complex64: 5-qubit blocks as 3xTF32 tensor-core GEMMs, FP32 accumulation."""
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    ops = flatten(layered_circuit(n, 8, 500 + n)) + mixed_circuit(np.random.default_rng(n), n, 60)
+    o = OracleRegister.from_int(n, 0)
+    o.apply_sequence([(g.matrix, g.targets) for g in ops])
+    for w in (5, 3):
+        g = q.Register.from_int(n, 0, precision=1)
+        g.apply_gates(ops, fuse=2, max_width=w)
+        st = g.state
+        assert floored_rel_err(st, o.state) <= 2e-5, w
+        f = abs(np.vdot(st, o.state)) ** 2 / (np.vdot(st, st).real * np.vdot(o.state, o.state).real)
+        assert 1 - f <= 1e-9, w
+
+
+def test_dense_block_fusion_c128_and_small_registers():
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+
+    for n, prec, tol in ((13, 0, 1e-12), (7, 1, 2e-5), (5, 0, 1e-12)):
+        ops = mixed_circuit(np.random.default_rng(n + 7), n, 150)
+        o = OracleRegister.from_int(n, 0)
+        o.apply_sequence([(g.matrix, g.targets) for g in ops])
+        g = q.Register.from_int(n, 0, precision=prec)
+        g.set_arith(1)
+        g.apply_gates(ops, fuse=2)
+        assert floored_rel_err(g.state, o.state) <= tol, (n, prec)

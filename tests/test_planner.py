@@ -78,3 +78,44 @@ def test_planned_tiles_match_oracle(emulator, oracle_mod, T, L):
         assert stages < len(ops), name
         bad = np.nonzero(~((got.view(np.float64) == o.state.view(np.float64))))[0]
         assert bad.size == 0, f"{name}: {bad.size} values differ, first at {bad[:4]}"
+
+
+FUSE_SRC = ROOT / "tests" / "cpp" / "fuse_check.cpp"
+FUSE_EXE = ROOT / "tests" / "cpp" / "_build" / "fuse_check"
+
+
+@pytest.fixture(scope="module")
+def fuser():
+    FUSE_EXE.parent.mkdir(exist_ok=True)
+    srcs = [FUSE_SRC, ROOT / "quaru_gb300/csrc/qs_fuse.cpp"]
+    if not FUSE_EXE.exists() or FUSE_EXE.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
+        subprocess.run(["g++", "-O1", "-std=c++17", "-I", str(ROOT / "include"), *map(str, srcs), "-o",
+                        str(FUSE_EXE)], check=True)
+    return FUSE_EXE
+
+
+@pytest.mark.parametrize("W", [2, 3, 5])
+def test_fused_blocks_reproduce_gate_by_gate(fuser, oracle_mod, W):
+    from quaru_gb300.operation import Operation
+
+    for name, n, ops in cases():
+        if name == "controls":  # include a gate wider than W
+            ops = ops + [Operation(np.eye(64, dtype=complex)[np.random.default_rng(1).permutation(64)],
+                                   [0, 2, 4, 6, 8, 10])]
+        rng = np.random.default_rng(len(ops) + W)
+        st = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        st /= np.linalg.norm(st)
+        buf = bytearray(struct.pack("<3i", n, W, len(ops)))
+        for op in ops:
+            t = list(op.targets)
+            buf += struct.pack("<i", len(t)) + struct.pack(f"<{len(t)}i", *t)
+            buf += np.ascontiguousarray(np.asarray(op.matrix, dtype=np.complex128)).tobytes()
+        buf += np.ascontiguousarray(st, dtype=np.complex128).tobytes()
+        r = subprocess.run([str(fuser)], input=bytes(buf), capture_output=True, check=True)
+        got = np.frombuffer(r.stdout[: 16 << n], dtype=np.complex128)
+        nblocks = struct.unpack("<i", r.stdout[16 << n:])[0]
+        o = oracle_mod.OracleRegister.from_int(n, 0)
+        o.state = st.copy()
+        o.apply_sequence([(g.matrix, g.targets) for g in ops])
+        assert nblocks < len(ops)
+        assert np.max(np.abs(got - o.state)) < 1e-12, name
