@@ -205,6 +205,46 @@ int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, 
                         size_t nparams, const qs_pauli_term* terms, size_t nterms, double* energy,
                         double* grad, size_t* err);
 
+/* ---- batched gradients (no counterpart in the reference) ------------------ */
+
+/* One circuit of a batch: n qubits starting in |0..0>, gates (rotations, fixed
+ * 1-qubit gates and CNOTs), its observable. */
+typedef struct qs_batch_circuit {
+    size_t n;
+    const qs_param_gate* gates;
+    size_t m;
+    size_t nparams;
+    const qs_pauli_term* terms;
+    size_t nterms;
+} qs_batch_circuit;
+
+typedef struct qs_batch_options {
+    int precision;       /* QS_PREC_C128 or QS_PREC_C64 */
+    int chunk_log2;      /* amplitude pairs per work item = 2^chunk_log2; 0 = autotune */
+    int ctas_per_sm;     /* persistent CTAs per SM; 0 = autotune */
+    int reserved;
+} qs_batch_options;
+
+typedef struct qs_batch qs_batch;
+
+/* Prepare a batch: device states, gate and observable tables, the work-item
+ * schedule, and a CUDA graph of the whole forward + adjoint pass (parameter
+ * upload, state reset, one persistent kernel over all circuits, the
+ * gradient reduction, result download). Validation errors carry err[2] =
+ * circuit index. */
+int qs_batch_create(const qs_batch_circuit* circuits, size_t count, const qs_batch_options* opts,
+                    qs_batch** out, size_t* err);
+
+/* Energies (count) and gradients (concatenated, nparams per circuit) for the
+ * given parameters (concatenated likewise): one graph replay. QS_TIMEOUT if a
+ * bounded dependency wait inside the persistent kernel gave up. */
+int qs_batch_run(qs_batch* batch, const double* params, double* energies, double* grads);
+
+/* The chunk size and CTAs per SM the batch runs with (after autotuning). */
+int qs_batch_config(const qs_batch* batch, int* chunk_log2, int* ctas_per_sm);
+
+void qs_batch_free(qs_batch* batch);
+
 /* ---- host views ---------------------------------------------------------- */
 
 /* Read `pub state` (src/register.rs:35): 2^n complex, interleaved doubles. */

@@ -59,6 +59,16 @@ class QsParamGate(ctypes.Structure):
 
 QS_GATE_FIXED, QS_GATE_RX, QS_GATE_RY, QS_GATE_RZ = 0, 1, 2, 3
 
+
+class QsBatchCircuit(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("gates", ctypes.POINTER(QsParamGate)), ("m", ctypes.c_size_t),
+                ("nparams", ctypes.c_size_t), ("terms", ctypes.POINTER(QsPauliTerm)), ("nterms", ctypes.c_size_t)]
+
+
+class QsBatchOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("chunk_log2", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
+
 SIGNATURES = {
     "qs_register_new": (_i, [_P(ctypes.c_uint8), _sz, _i, _P(_vp)]),
     "qs_register_from_int": (_i, [_sz, _sz, _i, _P(_vp)]),
@@ -77,6 +87,10 @@ SIGNATURES = {
     "qs_inner_product": (_i, [_vp, _vp, _dp, _dp]),
     "qs_expval_pauli": (_i, [_vp, _P(QsPauliTerm), _sz, _dp]),
     "qs_adjoint_gradient": (_i, [_vp, _P(QsParamGate), _sz, _dp, _sz, _P(QsPauliTerm), _sz, _dp, _dp, _sp]),
+    "qs_batch_create": (_i, [_P(QsBatchCircuit), _sz, _P(QsBatchOptions), _P(_vp), _sp]),
+    "qs_batch_run": (_i, [_vp, _dp, _dp, _dp]),
+    "qs_batch_config": (_i, [_vp, _P(_i), _P(_i)]),
+    "qs_batch_free": (None, [_vp]),
     "qs_get_state": (_i, [_vp, _dp]),
     "qs_set_state": (_i, [_vp, _dp]),
     "qs_probabilities": (_i, [_vp, _dp]),

@@ -1,0 +1,64 @@
+"""Batched forward + adjoint gradients for many circuits (one persistent launch in a CUDA graph)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .register import EngineError, OperationError, ParamGate, _check, _dp, _pauli_array, _sp
+
+
+class Batch:
+    """Circuits (ParamGate lists, parameter counts, Pauli observables) prepared once; run() replays the graph."""
+
+    def __init__(self, circuits, precision: int = _lib.QS_PREC_C128, chunk_log2: int = 0, ctas_per_sm: int = 0):
+        lib = _lib.load()
+        self._keep = []
+        arr = (_lib.QsBatchCircuit * max(1, len(circuits)))()
+        self.nparams = []
+        for i, (n, gates, nparams, terms) in enumerate(circuits):
+            cg = (_lib.QsParamGate * max(1, len(gates)))()
+            for k, g in enumerate(gates):
+                cg[k].kind = g.kind
+                cg[k].param = g.param
+                if g.kind == _lib.QS_GATE_FIXED:
+                    m = np.ascontiguousarray(np.asarray(g.op.matrix, dtype=np.complex128))
+                    t = np.ascontiguousarray(np.array(list(g.op.targets), dtype=np.uintp))
+                    cg[k].matrix = _dp(m.view(np.float64))
+                    self._keep.append(m)
+                else:
+                    t = np.ascontiguousarray(np.array([g.target], dtype=np.uintp))
+                cg[k].k = len(t)
+                cg[k].targets = _sp(t)
+                self._keep.append(t)
+            pt = _pauli_array(terms)
+            self._keep += [cg, pt]
+            arr[i].n, arr[i].gates, arr[i].m = n, cg, len(gates)
+            arr[i].nparams, arr[i].terms, arr[i].nterms = nparams, pt, len(terms)
+            self.nparams.append(nparams)
+        opts = _lib.QsBatchOptions(precision, chunk_log2, ctas_per_sm, 0)
+        h = ctypes.c_void_p()
+        err = np.zeros(3, dtype=np.uintp)
+        _check(lib.qs_batch_create(arr, len(circuits), ctypes.byref(opts), ctypes.byref(h), _sp(err)), err)
+        self._h = h
+        self.count = len(circuits)
+
+    def run(self, params):
+        """params: concatenated per circuit. Returns (energies[count], grads concatenated)."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float64))
+        e = np.zeros(self.count)
+        g = np.zeros(max(1, sum(self.nparams)))
+        _check(_lib.load().qs_batch_run(self._h, _dp(p), _dp(e), _dp(g)))
+        return e, g[: sum(self.nparams)]
+
+    def config(self):
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.load().qs_batch_config(self._h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.qs_batch_free(h)
+            self._h = ctypes.c_void_p()

@@ -303,8 +303,15 @@ int qs_inner_product(const qs_register* a, const qs_register* b, double* re, dou
     return QS_OK;
 }
 
+static bool terms_fit(const qs_pauli_term* terms, size_t nterms, int n) {
+    for (size_t t = 0; t < nterms; t++)
+        if (n < 64 && ((terms[t].x_mask | terms[t].z_mask) >> n)) return false;
+    return true;
+}
+
 int qs_expval_pauli(qs_register* reg, const qs_pauli_term* terms, size_t nterms, double* value) {
     if (!reg || !value || (nterms && !terms)) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    if (!terms_fit(terms, nterms, reg->n)) return set_err(QS_INVALID_ARGUMENT, "Pauli term acts on a qubit >= n");
     std::string msg;
     int rc = qs::expval_pauli(reg->state, reg->prec, reg->n, terms, nterms, reg->stream, reg->sms, value, &msg);
     return rc ? set_err(rc, msg) : QS_OK;
@@ -316,6 +323,7 @@ int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, 
     if ((m && !gates) || (nparams && !params) || (nterms && !terms))
         return set_err(QS_INVALID_ARGUMENT, "null argument");
     if (reg->n < 1) return set_err(QS_INVALID_ARGUMENT, "register has no qubits");
+    if (!terms_fit(terms, nterms, reg->n)) return set_err(QS_INVALID_ARGUMENT, "Pauli term acts on a qubit >= n");
     std::string msg;
     int rc = qs::adjoint_gradient(reg->state, reg->n, reg->prec, reg->arith, gates, m, params, nparams, terms, nterms,
                                   reg->stream, reg->sms, energy, grad, err, &msg);

@@ -167,3 +167,30 @@ def config4(n: int = 20, layers: int = 10, seed: int | None = None):
     gates, npar = ansatz(n, layers)
     params = [2.0 * math.pi * rng.uniform() for _ in range(npar)]
     return gates, params, chain_hamiltonian(n, rng)
+
+
+def config5(count: int = 256, qmin: int = 10, qmax: int = 22, lmin: int = 4, lmax: int = 12,
+            seed: int | None = None):
+    """Batch of ansatz circuits: qubits ~ U{qmin..qmax}, layers ~ U{lmin..lmax}, parameters ~ U[0, 2pi),
+    random Z / ZZ / X observables with N(0, 1) coefficients. Returns (circuits, params) where each circuit
+    is (n, gates, nparams, terms) and params is the concatenation."""
+    rng = SplitMix64(seed_for(5) if seed is None else seed)
+    circuits, params = [], []
+    for _ in range(count):
+        n = qmin + rng.randint(qmax - qmin + 1)
+        layers = lmin + rng.randint(lmax - lmin + 1)
+        gates, npar = ansatz(n, layers)
+        terms = []
+        for _ in range(n):
+            kind = rng.randint(3)
+            a = rng.randint(n)
+            if kind == 0:
+                terms.append((rng.normal(), 0, 1 << a))
+            elif kind == 1:
+                b = (a + 1 + rng.randint(n - 1)) % n
+                terms.append((rng.normal(), 0, (1 << a) | (1 << b)))
+            else:
+                terms.append((rng.normal(), 1 << a, 0))
+        circuits.append((n, gates, npar, terms))
+        params += [2.0 * math.pi * rng.uniform() for _ in range(npar)]
+    return circuits, params

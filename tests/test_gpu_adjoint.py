@@ -143,3 +143,7 @@ def test_adjoint_rejects_bad_gates():
     assert e.value.kind == "InvalidTarget" and e.value.payload == (5,)
     with pytest.raises(q.EngineError):
         reg.adjoint_gradient([ParamGate.ry(0, 3)], [0.1], [(1.0, 0, 1)])
+    with pytest.raises(q.EngineError):  # a Pauli term on qubit 3 of a 3-qubit register
+        reg.adjoint_gradient([ParamGate.ry(0, 0)], [0.1], [(1.0, 0b1000, 0)])
+    with pytest.raises(q.EngineError):
+        reg.expval_pauli([(1.0, 0, 0b10000)])
