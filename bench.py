@@ -299,6 +299,7 @@ def run_ours(args) -> None:
                                       "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0)}
 
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
+    batch = None if args.no_batch else batch_section(q, args)
 
     t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
     if dist:
@@ -353,6 +354,7 @@ def run_ours(args) -> None:
         "clocks": clk,
         "fused": fused,
         "adjoint": adjoint,
+        "batch": batch,
         "cpu_baseline": cpu,
         "probe": {"p0_qubit0": p0},
     }
@@ -396,6 +398,45 @@ def adjoint_section(q, torch, args) -> dict:
     return out
 
 
+def batch_section(q, args) -> dict:
+    """256 ansatz circuits (10..22 qubits, 4..12 layers): one persistent graph replay per run vs a loop of
+    single-circuit adjoint calls."""
+    from quaru_gb300.batch import Batch
+    from quaru_gb300.workloads import config5
+
+    circuits, params = config5()
+    params = np.array(params)
+    ngrads = len(params)
+    out = {"workload": "256 ansatz circuits, qubits ~ U{10..22}, layers ~ U{4..12}, random Z/ZZ/X observables",
+           "circuits": len(circuits), "parameters": ngrads}
+    for name, prec in (("fp64", q.QS_PREC_C128), ("mixed", q.QS_PREC_C64)):
+        t0 = time.perf_counter()
+        b = Batch(circuits, precision=prec)
+        setup = time.perf_counter() - t0
+        b.run(params)
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            e, g = b.run(params)
+        dt = (time.perf_counter() - t0) / reps
+        cl, ct = b.config()
+        out[name] = {"s_per_batch": dt, "circuits_per_s": len(circuits) / dt, "grads_per_s": ngrads / dt,
+                     "setup_s_incl_autotune": setup, "chunk_log2": cl, "ctas_per_sm": ct}
+        del b
+    # the plain loop: one qs_adjoint_gradient call per circuit (FP64)
+    t0 = time.perf_counter()
+    off = 0
+    for n, gates, npar, terms in circuits:
+        reg = q.Register.from_int(n, 0)
+        reg.set_arith(q.QS_ARITH_FMA)
+        reg.adjoint_gradient(gates, params[off:off + npar], terms)
+        off += npar
+    loop = time.perf_counter() - t0
+    out["loop_fp64"] = {"s_per_batch": loop, "circuits_per_s": len(circuits) / loop, "grads_per_s": ngrads / loop}
+    out["batch_vs_loop_fp64"] = loop / out["fp64"]["s_per_batch"]
+    return out
+
+
 def _measure_probs(lib, reg, target: int) -> float:
     import ctypes
 
@@ -421,6 +462,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused (tiled) circuit timing")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-gradient section")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")
