@@ -39,6 +39,8 @@ extern "C" {
 #define QS_CUDA_ERROR 6         /* a CUDA runtime call failed */
 #define QS_OUT_OF_MEMORY 7      /* device allocation failed */
 #define QS_TIMEOUT 8            /* a bounded device wait gave up */
+#define QS_QASM_PARSE_ERROR 9   /* OpenQASMError::OpenQASMParseError */
+#define QS_QASM_RUN_ERROR 10    /* OpenQASMError::OpenQASMRunError */
 
 /* ---- state precision ---------------------------------------------------- */
 #define QS_PREC_C128 0 /* complex128 state (the reference's c64 = Complex<f64>) */
@@ -244,6 +246,35 @@ int qs_batch_run(qs_batch* batch, const double* params, double* energies, double
 int qs_batch_config(const qs_batch* batch, int* chunk_log2, int* ctas_per_sm);
 
 void qs_batch_free(qs_batch* batch);
+
+/* ---- OpenQASM 2.0 front end ---------------------------------------------- */
+
+typedef struct qs_qasm_result qs_qasm_result;
+
+/* openqasm::run_openqasm (src/openqasm.rs:52-142) on program text: one
+ * register per qreg (all |0..0>), bits per creg; U, CX, measure, reset,
+ * barrier, if(creg == n), gate definitions and the standard gates of
+ * "qelib1.inc". Measurement draws come from a SplitMix64 generator seeded with
+ * `seed` (the reference uses an unseeded thread_rng). Includes other than
+ * qelib1.inc are read relative to base_dir (nullable). Errors:
+ * QS_QASM_PARSE_ERROR (syntax, unknown names, bad arguments) and
+ * QS_QASM_RUN_ERROR (CX across registers, a creg wider than 32 bits in an if),
+ * message in qs_last_error(). */
+int qs_qasm_run(const char* source, const char* base_dir, uint64_t seed, int precision, qs_qasm_result** out);
+
+/* As qs_qasm_run on the contents of a file (includes relative to its directory). */
+int qs_qasm_run_file(const char* path, uint64_t seed, int precision, qs_qasm_result** out);
+
+/* OpenQASMResult's qregs / cregs maps (src/openqasm.rs:9-16), in declaration
+ * order. Registers stay owned by the result. */
+size_t qs_qasm_qreg_count(const qs_qasm_result* result);
+const char* qs_qasm_qreg_name(const qs_qasm_result* result, size_t i);
+qs_register* qs_qasm_qreg(qs_qasm_result* result, size_t i);
+size_t qs_qasm_creg_count(const qs_qasm_result* result);
+const char* qs_qasm_creg_name(const qs_qasm_result* result, size_t i);
+size_t qs_qasm_creg_size(const qs_qasm_result* result, size_t i);
+int qs_qasm_creg_bits(const qs_qasm_result* result, size_t i, uint8_t* bits);
+void qs_qasm_free(qs_qasm_result* result);
 
 /* ---- host views ---------------------------------------------------------- */
 

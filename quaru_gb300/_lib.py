@@ -22,6 +22,8 @@ QS_INVALID_ARGUMENT = 5
 QS_CUDA_ERROR = 6
 QS_OUT_OF_MEMORY = 7
 QS_TIMEOUT = 8
+QS_QASM_PARSE_ERROR = 9
+QS_QASM_RUN_ERROR = 10
 
 QS_PREC_C128 = 0
 QS_PREC_C64 = 1
@@ -91,6 +93,16 @@ SIGNATURES = {
     "qs_batch_run": (_i, [_vp, _dp, _dp, _dp]),
     "qs_batch_config": (_i, [_vp, _P(_i), _P(_i)]),
     "qs_batch_free": (None, [_vp]),
+    "qs_qasm_run": (_i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint64, _i, _P(_vp)]),
+    "qs_qasm_run_file": (_i, [ctypes.c_char_p, ctypes.c_uint64, _i, _P(_vp)]),
+    "qs_qasm_qreg_count": (_sz, [_vp]),
+    "qs_qasm_qreg_name": (ctypes.c_char_p, [_vp, _sz]),
+    "qs_qasm_qreg": (_vp, [_vp, _sz]),
+    "qs_qasm_creg_count": (_sz, [_vp]),
+    "qs_qasm_creg_name": (ctypes.c_char_p, [_vp, _sz]),
+    "qs_qasm_creg_size": (_sz, [_vp, _sz]),
+    "qs_qasm_creg_bits": (_i, [_vp, _sz, _P(ctypes.c_uint8)]),
+    "qs_qasm_free": (None, [_vp]),
     "qs_get_state": (_i, [_vp, _dp]),
     "qs_set_state": (_i, [_vp, _dp]),
     "qs_probabilities": (_i, [_vp, _dp]),

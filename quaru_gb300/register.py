@@ -189,6 +189,21 @@ class Register:
         _check(rc, err)
         return self
 
+    def apply_circuit(self, circuit, fuse: int = 0) -> list:
+        """Register::apply_circuit (src/register.rs:345-369): the gates (one library call), then the
+        measurements in order, then each conditional gate whose (target, value) conditions all hold."""
+        if circuit.get_operations():
+            self.apply_gates(circuit.get_operations(), fuse=fuse)
+        measures = self.measure_circuit(circuit) if circuit.get_measurement_targets() else []
+        for op, cond in circuit.get_conditional_operations():
+            if all((t, v) in measures for t, v in cond):
+                self.apply(op)
+        return measures
+
+    def measure_circuit(self, circuit) -> list:
+        """Register::measure_circuit (src/register.rs:371-377)."""
+        return [(t, self.measure(t)) for t in circuit.get_measurement_targets()]
+
     # ---- measurement (src/register.rs:291-342)
     def try_measure(self, target: int, draw: float | None = None) -> bool:
         x = self._rng() if draw is None else float(draw)
