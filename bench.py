@@ -447,6 +447,45 @@ def _measure_probs(lib, reg, target: int) -> float:
     return p0.value
 
 
+def run_kernels(args) -> None:
+    """A small workload that launches every kernel family once per repetition (for ncu captures):
+    init, dense 1-qubit (exact, FMA, DF64), CNOT/permutation, dense 3-qubit, probability reduction
+    and collapse, tiles (complex128 DF64, complex64 groups, complex64 3xTF32 blocks), adjoint, batch."""
+    import quaru_gb300 as q
+    from quaru_gb300 import operation as O
+    from quaru_gb300.batch import Batch
+    from quaru_gb300.workloads import config4, config5, flatten, layered_circuit
+
+    n = args.qubits
+    rng = np.random.default_rng(1)
+    layers = flatten(layered_circuit(n, 2, 7))
+    haar = [g for g in layers if len(g.targets) == 1][:3]
+    u3 = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0]
+    for rep in range(args.steps):
+        for arith in (q.QS_ARITH_EXACT, q.QS_ARITH_FMA, q.QS_ARITH_DF64):
+            r = q.Register.from_int(n, 0)
+            r.set_arith(arith)
+            for g in haar:
+                r.try_apply_fast(g)
+        r.try_apply_fast(O.cnot(3, n - 2))
+        r.try_apply_fast(O.cnx([1, 2], n - 1))
+        r.try_apply_fast(O.Operation(u3, [0, n // 2, n - 3]))
+        r.measure(n - 1, 0.5)
+        r.apply_gates(layers, fuse=1)
+        c = q.Register.from_int(n, 0, precision=q.QS_PREC_C64)
+        c.apply_gates(layers, fuse=1)
+        c.apply_gates(layers, fuse=2)
+        del r, c
+    gates, params, terms = config4()
+    reg = q.Register.from_int(20, 0)
+    reg.set_arith(q.QS_ARITH_FMA)
+    reg.adjoint_gradient(gates, params, terms)
+    circuits, bp = config5(count=16, qmin=10, qmax=18, lmin=2, lmax=4, seed=3)
+    b = Batch(circuits, chunk_log2=11, ctas_per_sm=2)
+    b.run(bp)
+    print(json.dumps({"kernels": "done", "qubits": n, "launches": int(q._lib.load().qs_launch_count())}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -463,11 +502,14 @@ def main() -> None:
     ap.add_argument("--no-fused", action="store_true", help="skip the fused (tiled) circuit timing")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-gradient section")
+    ap.add_argument("--kernels", action="store_true", help="run the per-kernel profiling workload instead")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")
     if args.impl == "reference":
         run_reference(args)
+    elif args.kernels:
+        run_kernels(args)
     else:
         run_ours(args)
 
