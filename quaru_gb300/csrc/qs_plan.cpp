@@ -254,6 +254,7 @@ std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStag
             prog.push_back(group_header(gbits, st.T, int(members.size())));
             for (TileOp m : members) {
                 m.gj = (m.k == 1) ? uint8_t(gl(m.tb[0])) : 0;
+                m.gcode = (m.kind == OP_DENSE) ? 0 : (m.kind == OP_DENSE_REAL) ? 1 : (m.k == 1) ? 2 : 3;
                 // local fixed bits: positions other than the target, with values in lfixval
                 for (int i = 0; i < m.npos; i++) {
                     const int lb = m.pos[i];

@@ -256,7 +256,9 @@ __device__ __forceinline__ void dense_pair(const DenseCoef<2>& c, bool real, flo
     b = make_float4(oh[2], ol[2], oh[3], ol[3]);
 }
 
-// ---- register groups: the 8 amplitudes of a 3-bit sub-cube held in registers
+// ---- register groups (complex64): each thread holds two 8-amplitude tuples of a 3-bit
+// sub-cube in registers and applies the group's members to both; a member's fields are read
+// once per pair of tuples and dispatched to code specialised for its target bit.
 template <int REP>
 __device__ __forceinline__ typename TileElem<REP>::T mono_row(const TileOp& m, int r, typename TileElem<REP>::T src) {
     const uint8_t c = m.pf[r];
@@ -264,48 +266,120 @@ __device__ __forceinline__ typename TileElem<REP>::T mono_row(const TileOp& m, i
     return pf_move(src, c);
 }
 
-// Pair (a, b) of a k = 1 gate on group-local bit j; a has bit j clear.
-template <int REP>
-__device__ __forceinline__ void group_pair(const TileOp& m, const DenseCoef<REP>& c, bool dense, bool real,
-                                           typename TileElem<REP>::T& xa, typename TileElem<REP>::T& xb) {
-    using E = typename TileElem<REP>::T;
-    if (dense) {
-        dense_pair(c, real, xa, xb);
-    } else {
-        const E s0 = m.offsrc[0] ? xb : xa;
-        const E s1 = m.offsrc[1] ? xb : xa;
-        if (m.pf[0] != PF_SKIP_DEV) xa = mono_row<REP>(m, 0, s0);
-        if (m.pf[1] != PF_SKIP_DEV) xb = mono_row<REP>(m, 1, s1);
+struct GMember {
+    float u[8];     // dense coefficients, or the two rows' phases for monomials
+    int fm, fv;     // fixed bits inside the group
+    uint8_t pf0, pf1, s0, s1;
+};
+
+__device__ __forceinline__ float2 gm_row(uint8_t cls, const float* ph, float2 x) {
+    if (cls == 255) return make_float2(fmaf(ph[0], x.x, -ph[1] * x.y), fmaf(ph[0], x.y, ph[1] * x.x));
+    return apply_pf(x, cls);
+}
+
+template <int J, int CODE, bool ALL>
+__device__ __forceinline__ void gm_apply(const GMember& g, float2 (&x)[8]) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+        if (a & (1 << J)) continue;
+        if (!ALL && ((a & g.fm) != g.fv)) continue;
+        const int b = a | (1 << J);
+        const float2 xa = x[a], xb = x[b];
+        if (CODE == 0) {
+            float2 y0 = cfma(g.u[2], g.u[3], xb, czero<float2>());
+            y0 = cfma(g.u[0], g.u[1], xa, y0);
+            float2 y1 = cfma(g.u[6], g.u[7], xb, czero<float2>());
+            y1 = cfma(g.u[4], g.u[5], xa, y1);
+            x[a] = y0;
+            x[b] = y1;
+        } else if (CODE == 1) {
+            float2 y0, y1;
+            y0.x = fmaf(g.u[0], xa.x, g.u[2] * xb.x);
+            y0.y = fmaf(g.u[0], xa.y, g.u[2] * xb.y);
+            y1.x = fmaf(g.u[4], xa.x, g.u[6] * xb.x);
+            y1.y = fmaf(g.u[4], xa.y, g.u[6] * xb.y);
+            x[a] = y0;
+            x[b] = y1;
+        } else {
+            const float2 s0 = g.s0 ? xb : xa, s1 = g.s1 ? xb : xa;
+            if (g.pf0 != PF_SKIP_DEV) x[a] = gm_row(g.pf0, g.u, s0);
+            if (g.pf1 != PF_SKIP_DEV) x[b] = gm_row(g.pf1, g.u + 2, s1);
+        }
     }
 }
 
-#define QS_GPAIR(A, B)                                                          \
-    if (((A) & fm) == fv) group_pair<REP>(m, c, dense, real, x[A], x[B]);
+template <int CODE, bool ALL>
+__device__ __forceinline__ void gm_dispatch_j(int j, const GMember& g, float2 (&x)[8]) {
+    if (j == 0)
+        gm_apply<0, CODE, ALL>(g, x);
+    else if (j == 1)
+        gm_apply<1, CODE, ALL>(g, x);
+    else
+        gm_apply<2, CODE, ALL>(g, x);
+}
 
-template <int REP>
-__device__ __forceinline__ void group_apply(const TileOp& m, typename TileElem<REP>::T (&x)[8]) {
-    const int fm = m.gfin_mask, fv = m.gfin_val;
-    const int kind = m.kind;
-    if (m.k == 0) {  // phase or sign on the fixed subspace
+__device__ __forceinline__ void gm_dispatch(int code, int j, const GMember& g, float2 (&x)[8]) {
+    const bool all = g.fm == 0;
+    if (code == 3) {  // phase or sign on the fixed subspace (k = 0)
+        if (g.pf0 == PF_SKIP_DEV) return;
 #pragma unroll
         for (int r = 0; r < 8; r++)
-            if ((r & fm) == fv && m.pf[0] != PF_SKIP_DEV) x[r] = mono_row<REP>(m, 0, x[r]);
+            if ((r & g.fm) == g.fv) x[r] = gm_row(g.pf0, g.u, x[r]);
         return;
     }
-    const bool dense = kind == OP_DENSE || kind == OP_DENSE_REAL;
-    const bool real = kind == OP_DENSE_REAL;
-    DenseCoef<REP> c;
-    if (dense) load_coef(c, m);
-    switch (m.gj) {
-        case 0:
-            QS_GPAIR(0, 1) QS_GPAIR(2, 3) QS_GPAIR(4, 5) QS_GPAIR(6, 7) break;
-        case 1:
-            QS_GPAIR(0, 2) QS_GPAIR(1, 3) QS_GPAIR(4, 6) QS_GPAIR(5, 7) break;
-        default:
-            QS_GPAIR(0, 4) QS_GPAIR(1, 5) QS_GPAIR(2, 6) QS_GPAIR(3, 7) break;
+    if (code == 0) {
+        if (all) gm_dispatch_j<0, true>(j, g, x); else gm_dispatch_j<0, false>(j, g, x);
+    } else if (code == 1) {
+        if (all) gm_dispatch_j<1, true>(j, g, x); else gm_dispatch_j<1, false>(j, g, x);
+    } else {
+        if (all) gm_dispatch_j<2, true>(j, g, x); else gm_dispatch_j<2, false>(j, g, x);
     }
 }
-#undef QS_GPAIR
+
+// One register group over the tile s (complex64). hdr is the OP_GROUP header, members follow it.
+__device__ __forceinline__ void group_run_c64(float2* s, uint32_t tsize, uint64_t base, const TileOp* hdr) {
+    const int cnt = hdr->k;
+    uint32_t goff[8], seg[5];
+#pragma unroll
+    for (int j = 0; j < 8; j++) goff[j] = hdr->off[j];
+#pragma unroll
+    for (int j = 0; j < 5; j++) seg[j] = hdr->seg[j];
+    const int npos = hdr->npos;
+    const uint32_t ng = tsize >> 3;
+    for (uint32_t p0 = threadIdx.x; p0 < ng; p0 += 2 * kTileThreads) {
+        const bool two = p0 + kTileThreads < ng;
+        const uint32_t b0 = tuple_index(p0, npos, seg, hdr->pos, 0u);
+        const uint32_t b1 = two ? tuple_index(p0 + kTileThreads, npos, seg, hdr->pos, 0u) : b0;
+        float2 x0[8], x1[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            x0[j] = s[b0 + goff[j]];
+            x1[j] = s[b1 + goff[j]];
+        }
+        for (int mi = 1; mi <= cnt; mi++) {
+            const TileOp& m = hdr[mi];
+            if ((base & m.omask) != m.oval) continue;
+            GMember g;
+#pragma unroll
+            for (int i = 0; i < 8; i++) g.u[i] = m.mf[i];
+            g.fm = m.gfin_mask;
+            g.fv = m.gfin_val;
+            g.pf0 = m.pf[0];
+            g.pf1 = m.pf[1];
+            g.s0 = m.offsrc[0] != 0;
+            g.s1 = m.offsrc[1] != 0;
+            const int code = m.gcode, j = m.gj;
+            const uint32_t om = m.gfout_mask, ov = m.gfout_val;
+            if ((b0 & om) == ov) gm_dispatch(code, j, g, x0);
+            if (two && (b1 & om) == ov) gm_dispatch(code, j, g, x1);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            s[b0 + goff[j]] = x0[j];
+            if (two) s[b1 + goff[j]] = x1[j];
+        }
+    }
+}
 
 // ---- fused 5-qubit blocks on the tensor cores (complex64 tiles, 3xTF32)
 __device__ __forceinline__ uint32_t f2tf32(float x) {
@@ -389,17 +463,76 @@ __device__ __forceinline__ void block_apply(float* sf, uint32_t tsize, const Til
     }
 }
 
+// ---- TMA bulk copies and mbarriers
+__device__ __forceinline__ uint32_t saddr(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait for the phase of `parity` to complete, at most ~2 s of SM clocks.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > 4000000000LL) return false;
+    return true;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(saddr(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Element type of the state in global memory (the tile buffer holds it while a copy is in flight).
+template <int REP>
+struct GlobElem {
+    using T = double2;
+};
+template <>
+struct GlobElem<3> {
+    using T = float2;
+};
+
+// One CTA walks its tiles with two shared-memory buffers: while it applies the stage to tile i,
+// warp 0 has already issued the bulk row copies of tile i + 1 into the other buffer (completion
+// on an mbarrier with expect-tx); finished tiles go back with bulk stores. Waits are bounded and
+// set *err instead of hanging.
 template <int REP, bool BLK>
-__global__ void __launch_bounds__(kTileThreads, (REP == 3 && !BLK) ? 3 : 2) k_tile(void* __restrict__ state, uint64_t ntiles,
+__global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ state, uint64_t ntiles,
                                                        const __grid_constant__ StageArgs sa,
                                                        const TileOp* __restrict__ ops,
-                                                       const float4* __restrict__ bfrag) {
+                                                       const float4* __restrict__ bfrag, int* __restrict__ err) {
     using E = typename TileElem<REP>::T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    E* s = reinterpret_cast<E*>(smem_raw);
+    using GE = typename GlobElem<REP>::T;
+    static_assert(sizeof(E) == sizeof(GE), "tile element and state element must have the same size");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t tsize = 1u << sa.T;
+    E* bufs = reinterpret_cast<E*>(smem_raw);
     const int nrows = 1 << sa.H;
-    uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + (sizeof(E) << sa.T));
-    TileOp* sops = reinterpret_cast<TileOp*>(rowoff + nrows);
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + 2 * (sizeof(E) << sa.T));
+    uint64_t* mbar = rowoff + nrows;
+    TileOp* sops = reinterpret_cast<TileOp*>(mbar + 2);
+    __shared__ int s_abort;
     const int nops = sa.op_end - sa.op_begin;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
@@ -413,14 +546,49 @@ __global__ void __launch_bounds__(kTileThreads, (REP == 3 && !BLK) ? 3 : 2) k_ti
             if (r >> b & 1) o |= 1ull << sa.high[b];
         rowoff[r] = o;
     }
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+        s_abort = 0;
+    }
     __syncthreads();
-    const uint32_t tsize = 1u << sa.T;
-    const uint32_t lmask = (1u << sa.L) - 1u;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const uint64_t base = expand_index(tile, sa.outer);
-        for (uint32_t i = threadIdx.x; i < tsize; i += kTileThreads)
-            s[i] = tile_load<REP>(state, base + rowoff[i >> sa.L] + (i & lmask));
+    const uint64_t first = blockIdx.x;
+    const uint64_t nmy = (ntiles > first) ? (ntiles - 1 - first) / gridDim.x + 1 : 0;
+    const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.L;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    GE* gstate = static_cast<GE*>(state);
+    auto issue_load = [&](uint64_t i, int b) {  // warp 0 only
+        const uint64_t tb = expand_index(first + i * gridDim.x, sa.outer);
+        if (lane == 0) mbar_expect_tx(&mbar[b], row_bytes * uint32_t(nrows));
+        __syncwarp();
+        for (int r = lane; r < nrows; r += 32)
+            bulk_load(bufs + size_t(b) * tsize + (size_t(r) << sa.L), gstate + tb + rowoff[r], row_bytes, &mbar[b]);
+    };
+    if (warp == 0 && nmy > 0) issue_load(0, 0);
+    uint64_t it = 0;
+    for (; it < nmy; it++) {
+        const int bsel = int(it & 1);
+        E* s = bufs + size_t(bsel) * tsize;
+        const uint64_t base = expand_index(first + it * gridDim.x, sa.outer);
+        if (warp == 0 && it + 1 < nmy) {
+            bulk_wait_read_all();  // the other buffer's previous store has read shared memory
+            __syncwarp();
+            issue_load(it + 1, bsel ^ 1);
+        }
+        if (!mbar_wait_bounded(&mbar[bsel], uint32_t((it >> 1) & 1))) atomicOr(&s_abort, 1);
         __syncthreads();
+        if (s_abort) break;
+        if constexpr (REP == 2) {  // split the loaded doubles into double-float pairs, in place
+            for (uint32_t i = threadIdx.x; i < tsize; i += kTileThreads) {
+                const double2 v = reinterpret_cast<const double2*>(s)[i];
+                float4 f;
+                df_split(v.x, f.x, f.y);
+                df_split(v.y, f.z, f.w);
+                s[i] = f;
+            }
+            __syncthreads();
+        }
         for (int o = 0; o < nops; o++) {
             const TileOp& op = sops[o];
             if ((base & op.omask) != op.oval) continue;
@@ -435,27 +603,8 @@ __global__ void __launch_bounds__(kTileThreads, (REP == 3 && !BLK) ? 3 : 2) k_ti
                 if constexpr (REP == 3 && BLK)
                     if (kind == OP_BLOCK) block_apply(reinterpret_cast<float*>(s), tsize, op, bfrag);
             } else if (REP == 3 && kind == OP_GROUP) {
-              if constexpr (REP == 3 && !BLK) {
-                const int cnt = op.k;
-                uint32_t goff[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) goff[j] = op.off[j];
-                for (uint32_t p = threadIdx.x; p < ntup; p += kTileThreads) {
-                    const uint32_t b0 = tuple_index(p, npos, seg, op.pos, 0u);
-                    E x[8];
-#pragma unroll
-                    for (int j = 0; j < 8; j++) x[j] = s[b0 + goff[j]];
-                    for (int mi = 1; mi <= cnt; mi++) {
-                        const TileOp& m = sops[o + mi];
-                        if ((base & m.omask) != m.oval) continue;
-                        if ((b0 & m.gfout_mask) != m.gfout_val) continue;
-                        group_apply<REP>(m, x);
-                    }
-#pragma unroll
-                    for (int j = 0; j < 8; j++) s[b0 + goff[j]] = x[j];
-                }
-                o += cnt;
-              }
+                if constexpr (REP == 3 && !BLK) group_run_c64(reinterpret_cast<float2*>(s), tsize, base, &sops[o]);
+                o += op.k;
             } else if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
                 const uint32_t tb = op.off[1];
                 const bool real = kind == OP_DENSE_REAL;
@@ -485,9 +634,25 @@ __global__ void __launch_bounds__(kTileThreads, (REP == 3 && !BLK) ? 3 : 2) k_ti
             }
             __syncthreads();
         }
-        for (uint32_t i = threadIdx.x; i < tsize; i += kTileThreads)
-            tile_store<REP>(state, base + rowoff[i >> sa.L] + (i & lmask), s[i]);
+        if constexpr (REP == 2) {  // join the double-float pairs back into doubles, in place
+            for (uint32_t i = threadIdx.x; i < tsize; i += kTileThreads) {
+                const float4 f = s[i];
+                reinterpret_cast<double2*>(s)[i] =
+                    make_double2(__dadd_rn(df_f2d(f.x), df_f2d(f.y)), __dadd_rn(df_f2d(f.z), df_f2d(f.w)));
+            }
+        }
+        fence_async_shared();  // make this tile's shared-memory writes visible to the bulk stores
         __syncthreads();
+        if (warp == 0) {
+            for (int r = lane; r < nrows; r += 32)
+                bulk_store(gstate + base + rowoff[r], s + (size_t(r) << sa.L), row_bytes);
+            bulk_commit();
+        }
+    }
+    if (warp == 0) bulk_wait_all();
+    if (s_abort && threadIdx.x == 0) {
+        atomicExch(err, 1);
+        if (it + 1 < nmy) mbar_wait_bounded(&mbar[int((it + 1) & 1)], uint32_t(((it + 1) >> 1) & 1));
     }
 }
 
@@ -498,7 +663,7 @@ static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
 
 template <int REP, bool BLK>
 static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_begin, int op_end,
-                               const TileOp* dops, const float4* dfrag, cudaStream_t s, int sms) {
+                               const TileOp* dops, const float4* dfrag, int* derr, cudaStream_t s, int sms) {
     using E = typename TileElem<REP>::T;
     StageArgs sa;
     std::memset(&sa, 0, sizeof(sa));
@@ -515,7 +680,8 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     for (size_t i = 0; i < qpos.size(); i++) sa.outer.pos[i] = uint8_t(qpos[i]);
     sa.outer.fixval = 0;
     for (int b = 0; b < sa.H; b++) sa.high[b] = uint8_t(st.high[b]);
-    const size_t smem = (sizeof(E) << st.T) + (sizeof(uint64_t) << sa.H) + sizeof(TileOp) * size_t(op_end - op_begin);
+    const size_t smem = 2 * (sizeof(E) << st.T) + (sizeof(uint64_t) << sa.H) + 2 * sizeof(uint64_t) +
+                        sizeof(TileOp) * size_t(op_end - op_begin);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_tile<REP, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
@@ -523,7 +689,7 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     const uint64_t ntiles = 1ull << (n - st.T);
     const int per_sm = std::max(1, std::min(8, int((220 * 1024) / smem)));
     const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * per_sm);
-    k_tile<REP, BLK><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, dfrag);
+    k_tile<REP, BLK><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, dfrag, derr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) note_launches(1);
     return e;
@@ -554,13 +720,21 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         // FP64 and double-float tiles are arithmetic-bound and keep one pass per gate.
         for (const TileOp& t : stage_program(ops, stages[i], rep == 3)) host.push_back(t);
     }
+    // One allocation: the op table, then an error flag the tile kernels raise when a bounded wait gives up.
     TileOp* dops = nullptr;
-    if (!host.empty()) {
-        cudaError_t e = cudaMallocAsync((void**)&dops, host.size() * sizeof(TileOp), s);
+    int* derr = nullptr;
+    unsigned char* dblob = nullptr;
+    const size_t ops_bytes = ((host.size() * sizeof(TileOp) + 255) / 256) * 256;
+    {
+        cudaError_t e = cudaMallocAsync((void**)&dblob, ops_bytes + 256, s);
         if (e != cudaSuccess) return tile_fail(e, "tile op table", msg);
-        e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(TileOp), cudaMemcpyHostToDevice, s);
+        dops = reinterpret_cast<TileOp*>(dblob);
+        derr = reinterpret_cast<int*>(dblob + ops_bytes);
+        e = cudaMemsetAsync(derr, 0, sizeof(int), s);
+        if (e == cudaSuccess && !host.empty())
+            e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(TileOp), cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) {
-            cudaFreeAsync(dops, s);
+            cudaFreeAsync(dblob, s);
             return tile_fail(e, "tile op upload", msg);
         }
     }
@@ -571,7 +745,7 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
             e = cudaMemcpyAsync(dfrag, block_frags->data(), block_frags->size() * sizeof(float),
                                 cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) {
-            if (dops) cudaFreeAsync(dops, s);
+            cudaFreeAsync(dblob, s);
             return tile_fail(e, "block fragments", msg);
         }
     }
@@ -585,19 +759,30 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         const int b = first[i], e2 = (i + 1 < stages.size()) ? first[i + 1] : int(host.size());
         cudaError_t e;
         switch (rep) {
-            case 0: e = launch_tile<0, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
-            case 1: e = launch_tile<1, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
-            case 2: e = launch_tile<2, false>(state, n, st, b, e2, dops, dfrag, s, sms); break;
+            case 0: e = launch_tile<0, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
+            case 1: e = launch_tile<1, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
+            case 2: e = launch_tile<2, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
             default:
                 if (dfrag)
-                    e = launch_tile<3, true>(state, n, st, b, e2, dops, dfrag, s, sms);
+                    e = launch_tile<3, true>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
                 else
-                    e = launch_tile<3, false>(state, n, st, b, e2, dops, dfrag, s, sms);
+                    e = launch_tile<3, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
                 break;
         }
         if (e != cudaSuccess) rc = tile_fail(e, "tile kernel", msg);
     }
-    if (dops) cudaFreeAsync(dops, s);
+    if (rc == QS_OK) {  // a bounded wait inside a tile kernel that gave up is reported here
+        int herr = 0;
+        cudaError_t e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            rc = tile_fail(e, "tile status", msg);
+        else if (herr) {
+            if (msg) *msg = "a tile kernel's bounded wait for its bulk copies gave up";
+            rc = QS_TIMEOUT;
+        }
+    }
+    cudaFreeAsync(dblob, s);
     if (dfrag) cudaFreeAsync(dfrag, s);
     return rc;
 }

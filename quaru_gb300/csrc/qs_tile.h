@@ -42,7 +42,7 @@ struct TileOp {
     uint8_t gj;          // group-local target bit (0..2)
     uint8_t gfin_mask;   // fixed bits inside the group (group-local)
     uint8_t gfin_val;
-    uint8_t pad_;
+    uint8_t gcode;       // 0 dense, 1 dense real, 2 monomial k = 1, 3 phase on a fixed subspace (k = 0)
     uint32_t gfout_mask; // fixed bits inside the tile but outside the group (tile-local)
     uint32_t gfout_val;
     uint32_t bidx;       // OP_BLOCK: offset of the block's B fragments (float4 units)
