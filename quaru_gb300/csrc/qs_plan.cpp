@@ -202,95 +202,235 @@ void block_fragments(const std::vector<double>& u, float* out) {
             }
 }
 
-// Whether a tile op can join a register group (k <= 1 dense or monomial).
-static bool groupable(const TileOp& t) {
-    if (t.kind == OP_DENSE || t.kind == OP_DENSE_REAL) return t.k == 1;
-    if (t.kind == OP_MONO || t.kind == OP_MONO_PF) return t.k <= 1;
+// Whether a stage op can be a register-pass member (k <= 1 dense or monomial).
+static bool passable(const OpDesc& op) {
+    if (op.kind == OP_DENSE || op.kind == OP_DENSE_REAL) return op.k == 1;
+    if (op.kind == OP_MONO || op.kind == OP_MONO_PF) return op.k <= 1;
     return false;
 }
 
-static TileOp group_header(uint32_t gbits, int T, int count) {
+static TileOp pass_header(const int (&r)[kPassBits], int entries) {
     TileOp h;
     std::memset(&h, 0, sizeof(h));
-    h.kind = OP_GROUP;
-    h.k = uint8_t(count);
-    std::vector<int> pos;
-    for (int b = 0; b < T; b++)
-        if (gbits >> b & 1u) pos.push_back(b);
-    h.npos = uint8_t(pos.size());
-    for (size_t i = 0; i < pos.size(); i++) h.pos[i] = uint8_t(pos[i]);
+    h.kind = OP_PASS;
+    h.k = uint8_t(entries);
+    h.npos = uint8_t(kPassBits);
+    for (int i = 0; i < kPassBits; i++) h.pos[i] = uint8_t(r[i]);
     int lo = 0;
-    for (size_t j = 0; j <= pos.size(); j++) {
-        const int hi = (j < pos.size()) ? pos[j] : 32;
+    for (int j = 0; j <= kPassBits; j++) {
+        const int hi = (j < kPassBits) ? r[j] : 32;
         uint32_t m = 0;
         for (int b = lo; b < hi && b < 32; b++) m |= 1u << b;
         h.seg[j] = m;
         lo = hi + 1;
     }
-    for (int j = 0; j < (1 << kGroupBits); j++) {
+    for (int j = 0; j < 16; j++) {  // register j's offset: the bits of j deposited on R
         uint32_t o = 0;
-        for (int b = 0; b < kGroupBits; b++)
-            if (j >> b & 1) o |= 1u << pos[b];
-        h.off[j] = o;
+        for (int b = 0; b < kPassBits; b++)
+            if (j >> b & 1) o |= 1u << r[b];
+        (j < 8 ? h.off[j] : h.offsrc[j - 8]) = o;
     }
     return h;
 }
 
-std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& st, bool groups) {
-    std::vector<TileOp> prog, members;
-    uint32_t gbits = 0;
-    auto flush = [&]() {
-        if (members.size() >= 2) {
-            // pad the group to exactly kGroupBits tile bits
-            for (int b = 0; b < st.T && __builtin_popcount(gbits) < kGroupBits; b++) gbits |= 1u << b;
-            std::vector<int> pos;
-            for (int b = 0; b < st.T; b++)
-                if (gbits >> b & 1u) pos.push_back(b);
-            auto gl = [&](int lb) -> int {
-                for (size_t i = 0; i < pos.size(); i++)
-                    if (pos[i] == lb) return int(i);
-                return -1;
-            };
-            prog.push_back(group_header(gbits, st.T, int(members.size())));
-            for (TileOp m : members) {
-                m.gj = (m.k == 1) ? uint8_t(gl(m.tb[0])) : 0;
-                m.gcode = (m.kind == OP_DENSE) ? 0 : (m.kind == OP_DENSE_REAL) ? 1 : (m.k == 1) ? 2 : 3;
-                // local fixed bits: positions other than the target, with values in lfixval
-                for (int i = 0; i < m.npos; i++) {
-                    const int lb = m.pos[i];
-                    if (m.k == 1 && lb == m.tb[0]) continue;
-                    const bool one = (m.lfixval >> lb) & 1u;
-                    const int j = gl(lb);
-                    if (j >= 0) {
-                        m.gfin_mask |= uint8_t(1u << j);
-                        if (one) m.gfin_val |= uint8_t(1u << j);
-                    } else {
-                        m.gfout_mask |= 1u << lb;
-                        if (one) m.gfout_val |= 1u << lb;
-                    }
-                }
-                prog.push_back(m);
-            }
-        } else {
-            for (const TileOp& m : members) prog.push_back(m);
-        }
-        members.clear();
-        gbits = 0;
+// Member entry of a pass gate t (a tile op of kind dense / monomial, k <= 1) for register bits r.
+static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
+    auto rix = [&](int lb) -> int {
+        for (int i = 0; i < kPassBits; i++)
+            if (r[i] == lb) return i;
+        return -1;
     };
-    for (int idx : st.ops) {
-        TileOp t = make_tile_op(ops[idx], st);
-        if (groups && st.T >= kGroupBits && groupable(t)) {
-            const uint32_t need = (t.k == 1) ? (1u << t.tb[0]) : 0u;
-            if (__builtin_popcount(gbits | need) > kGroupBits) flush();
-            gbits |= need;
-            members.push_back(t);
+    PassMember& pm = t.pm;
+    std::memset(&pm, 0, sizeof(pm));
+    uint32_t fm = 0, fv = 0;
+    for (int i = 0; i < t.npos; i++) {
+        const int lb = t.pos[i];
+        if (t.k == 1 && lb == t.tb[0]) continue;
+        const bool one = (t.lfixval >> lb) & 1u;
+        const int j = rix(lb);
+        if (j >= 0) {
+            fm |= 1u << j;
+            if (one) fv |= 1u << j;
         } else {
-            flush();
-            prog.push_back(t);
+            pm.om |= 1u << lb;
+            if (one) pm.ov |= 1u << lb;
         }
     }
-    flush();
+    pm.fmv = fm | (fv << 4);
+    const uint32_t all = fm == 0 ? 1u : 0u, nocond = pm.om == 0 ? 1u : 0u;
+    uint32_t vid, lane = 0;
+    if (t.k == 0) {  // phase on the rows matching the controls
+        vid = kPvPhase + all;
+        pm.u[0] = float(t.m[0]);
+        pm.u[1] = float(t.m[1]);
+    } else {
+        uint32_t code;
+        if (t.kind == OP_DENSE) {
+            code = PC_DENSE;
+            for (int i = 0; i < 8; i++) pm.u[i] = float(t.m[i]);
+        } else if (t.kind == OP_DENSE_REAL) {
+            code = PC_REAL;
+            for (int i = 0; i < 4; i++) pm.u[i] = float(t.m[2 * i]);
+        } else {
+            // k = 1 monomial of a unitary: the rows exchanged (X, Y, CNOT) or kept (RZ), each with
+            // a factor; the classifier drops untouched rows, so both rows are touched here.
+            const bool swapped = t.offsrc[0] != 0;
+            bool ones = true;
+            for (int row = 0; row < 2; row++) {
+                pm.u[2 * row] = float(t.m[2 * row]);
+                pm.u[2 * row + 1] = float(t.m[2 * row + 1]);
+                if (t.pf[row] != PF_ONE) ones = false;
+            }
+            code = swapped ? (ones ? PC_SWAP : PC_SWAPPH) : PC_DIAG2;
+        }
+        const int lb = t.tb[0];
+        if (lb < kLaneBits) {
+            lane = uint32_t(lb);
+            vid = kPvLane + code * 4 + all * 2 + nocond;
+        } else {
+            const uint32_t J = uint32_t(rix(lb));
+            vid = code * 8 + J * 2 + all;
+            // CNOT with its control on another register bit: a fixed register permutation
+            if (code == PC_SWAP && __builtin_popcount(fm) == 1 && fv == fm)
+                vid = kPvSwapC + J * 4 + uint32_t(__builtin_ctz(fm));
+        }
+    }
+    pm.ctl = vid | (lane << 10) | (t.omask ? (1u << 12) : 0u) | (pm.om ? (1u << 13) : 0u);
+    return t;
+}
+
+// Whether member entry e is a single dense gate on a register bit with no controls of any kind.
+static bool plain_dense(const TileOp& e, int* J) {
+    const uint32_t vid = e.pm.ctl & 255u;
+    if (vid >= 8 || !(vid & 1u) || (e.pm.ctl & ((1u << 12) | (1u << 13)))) return false;
+    *J = int(vid >> 1);
+    return true;
+}
+
+// Emits a pass: header, then the members with runs of plain dense gates on distinct register bits
+// merged into one multi-gate entry (bits in increasing order; such gates commute).
+static void emit_pass(const int (&r)[kPassBits], const std::vector<TileOp>& members, std::vector<TileOp>& prog) {
+    std::vector<TileOp> out;
+    for (size_t i = 0; i < members.size();) {
+        int J;
+        if (!plain_dense(members[i], &J)) {
+            out.push_back(members[i++]);
+            continue;
+        }
+        uint32_t mask = 0;
+        std::vector<const TileOp*> byj(kPassBits, nullptr);
+        size_t k = i;
+        while (k < members.size() && plain_dense(members[k], &J) && !(mask >> J & 1u)) {
+            mask |= 1u << J;
+            byj[J] = &members[k];
+            k++;
+        }
+        if (__builtin_popcount(mask) < 2) {
+            out.push_back(members[i++]);
+            continue;
+        }
+        bool head = true;
+        for (int j = 0; j < kPassBits; j++) {
+            if (!byj[j]) continue;
+            TileOp e = *byj[j];
+            if (head) e.pm.ctl = (kPvMulti + mask) | (uint32_t(__builtin_popcount(mask) - 1) << 8);
+            head = false;
+            out.push_back(e);
+        }
+        i = k;
+    }
+    prog.push_back(pass_header(r, int(out.size())));
+    for (const TileOp& e : out) prog.push_back(e);
+}
+
+static uint64_t op_qubits(const OpDesc& op) {
+    uint64_t m = op.fixmask;
+    for (int j = 0; j < op.k; j++) m |= 1ull << op.tq[j];
+    return m;
+}
+
+// Schedules a run of pass gates (stage-local indices into `seg`) into passes: each pass picks the
+// register bits that let the most gates run, a gate runs once every earlier gate sharing a qubit
+// with it has run, and gates keep their relative order within a pass.
+static void schedule_passes(const std::vector<OpDesc>& ops, const TileStage& st, const std::vector<int>& run,
+                            std::vector<TileOp>& prog) {
+    const int m = int(run.size());
+    std::vector<TileOp> tops(m);
+    std::vector<uint64_t> qm(m);
+    std::vector<int> tgt(m);
+    for (int i = 0; i < m; i++) {
+        tops[i] = make_tile_op(ops[run[i]], st);
+        qm[i] = op_qubits(ops[run[i]]);
+        tgt[i] = (tops[i].k == 1) ? tops[i].tb[0] : -1;
+    }
+    std::vector<char> done(m, 0);
+    int left = m;
+    std::vector<int> upper;
+    for (int b = kLaneBits; b < st.T; b++) upper.push_back(b);
+    const int U = int(upper.size());
+    while (left > 0) {
+        int best_count = -1, best_r[kPassBits] = {0, 0, 0, 0};
+        std::vector<int> best_sel;
+        for (uint32_t c = 0; c < (1u << U); c++) {
+            if (__builtin_popcount(c) != kPassBits) continue;
+            int r[kPassBits], ri = 0;
+            for (int i = 0; i < U; i++)
+                if (c >> i & 1u) r[ri++] = upper[i];
+            uint64_t blocked = 0;
+            std::vector<int> sel;
+            for (int i = 0; i < m; i++) {
+                if (done[i]) continue;
+                bool fits = tgt[i] < kLaneBits;
+                for (int j = 0; j < kPassBits && !fits; j++) fits = (r[j] == tgt[i]);
+                if (!fits || (qm[i] & blocked)) {
+                    blocked |= qm[i];
+                    continue;
+                }
+                sel.push_back(i);
+            }
+            if (int(sel.size()) > best_count) {
+                best_count = int(sel.size());
+                best_sel = sel;
+                std::copy(r, r + kPassBits, best_r);
+            }
+        }
+        std::vector<TileOp> members;
+        for (int i : best_sel) {
+            members.push_back(pass_member(tops[i], best_r));
+            done[i] = 1;
+            left--;
+        }
+        emit_pass(best_r, members, prog);
+    }
+}
+
+std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& st, bool passes) {
+    std::vector<TileOp> prog;
+    if (!passes || st.T < kPassMinT) {
+        for (int idx : st.ops) prog.push_back(make_tile_op(ops[idx], st));
+        return prog;
+    }
+    std::vector<int> run;
+    for (int idx : st.ops) {
+        const OpDesc& op = ops[idx];
+        if (op.kind == OP_NOOP) continue;
+        if (passable(op) && !(op.k == 0 && op.pf.size() && op.pf[0] == PF_SKIP)) {
+            run.push_back(idx);
+            continue;
+        }
+        if (!run.empty()) schedule_passes(ops, st, run, prog);
+        run.clear();
+        prog.push_back(make_tile_op(op, st));
+    }
+    if (!run.empty()) schedule_passes(ops, st, run, prog);
     return prog;
+}
+
+bool pass_only(const std::vector<TileOp>& prog) {
+    if (prog.empty()) return false;
+    for (size_t i = 0; i < prog.size(); i += size_t(prog[i].k) + 1)
+        if (prog[i].kind != OP_PASS) return false;
+    return true;
 }
 
 }  // namespace qs

@@ -22,6 +22,8 @@
 #include "qs_device.cuh"
 #include "qs_kernels.h"
 #include "qs_tile.h"
+#include "qs_pass.cuh"
+#include "qs_tma.cuh"
 
 namespace qs {
 
@@ -30,8 +32,10 @@ constexpr int kTileThreads = 256;
 struct StageArgs {
     int T, L, H;
     int op_begin, op_end;
+    int RL, RH;            // copy rows: 2^RL contiguous amplitudes, 2^RH rows per tile
+    int nbuf;              // tile buffers in the ring (2 or 3)
     IndexMap outer;        // expands a tile index into the base amplitude index
-    uint8_t high[kTileMaxHigh];  // global qubit of local bit L + b
+    uint8_t rhigh[kTileMaxHigh];  // global qubit of row bit b
 };
 
 template <int REP>
@@ -256,129 +260,11 @@ __device__ __forceinline__ void dense_pair(const DenseCoef<2>& c, bool real, flo
     b = make_float4(oh[2], ol[2], oh[3], ol[3]);
 }
 
-// ---- register groups (complex64): each thread holds two 8-amplitude tuples of a 3-bit
-// sub-cube in registers and applies the group's members to both; a member's fields are read
-// once per pair of tuples and dispatched to code specialised for its target bit.
 template <int REP>
 __device__ __forceinline__ typename TileElem<REP>::T mono_row(const TileOp& m, int r, typename TileElem<REP>::T src) {
     const uint8_t c = m.pf[r];
     if (c == 255) return phase_mul(m.m + 2 * r, src, REP);
     return pf_move(src, c);
-}
-
-struct GMember {
-    float u[8];     // dense coefficients, or the two rows' phases for monomials
-    int fm, fv;     // fixed bits inside the group
-    uint8_t pf0, pf1, s0, s1;
-};
-
-__device__ __forceinline__ float2 gm_row(uint8_t cls, const float* ph, float2 x) {
-    if (cls == 255) return make_float2(fmaf(ph[0], x.x, -ph[1] * x.y), fmaf(ph[0], x.y, ph[1] * x.x));
-    return apply_pf(x, cls);
-}
-
-template <int J, int CODE, bool ALL>
-__device__ __forceinline__ void gm_apply(const GMember& g, float2 (&x)[8]) {
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-        if (a & (1 << J)) continue;
-        if (!ALL && ((a & g.fm) != g.fv)) continue;
-        const int b = a | (1 << J);
-        const float2 xa = x[a], xb = x[b];
-        if (CODE == 0) {
-            float2 y0 = cfma(g.u[2], g.u[3], xb, czero<float2>());
-            y0 = cfma(g.u[0], g.u[1], xa, y0);
-            float2 y1 = cfma(g.u[6], g.u[7], xb, czero<float2>());
-            y1 = cfma(g.u[4], g.u[5], xa, y1);
-            x[a] = y0;
-            x[b] = y1;
-        } else if (CODE == 1) {
-            float2 y0, y1;
-            y0.x = fmaf(g.u[0], xa.x, g.u[2] * xb.x);
-            y0.y = fmaf(g.u[0], xa.y, g.u[2] * xb.y);
-            y1.x = fmaf(g.u[4], xa.x, g.u[6] * xb.x);
-            y1.y = fmaf(g.u[4], xa.y, g.u[6] * xb.y);
-            x[a] = y0;
-            x[b] = y1;
-        } else {
-            const float2 s0 = g.s0 ? xb : xa, s1 = g.s1 ? xb : xa;
-            if (g.pf0 != PF_SKIP_DEV) x[a] = gm_row(g.pf0, g.u, s0);
-            if (g.pf1 != PF_SKIP_DEV) x[b] = gm_row(g.pf1, g.u + 2, s1);
-        }
-    }
-}
-
-template <int CODE, bool ALL>
-__device__ __forceinline__ void gm_dispatch_j(int j, const GMember& g, float2 (&x)[8]) {
-    if (j == 0)
-        gm_apply<0, CODE, ALL>(g, x);
-    else if (j == 1)
-        gm_apply<1, CODE, ALL>(g, x);
-    else
-        gm_apply<2, CODE, ALL>(g, x);
-}
-
-__device__ __forceinline__ void gm_dispatch(int code, int j, const GMember& g, float2 (&x)[8]) {
-    const bool all = g.fm == 0;
-    if (code == 3) {  // phase or sign on the fixed subspace (k = 0)
-        if (g.pf0 == PF_SKIP_DEV) return;
-#pragma unroll
-        for (int r = 0; r < 8; r++)
-            if ((r & g.fm) == g.fv) x[r] = gm_row(g.pf0, g.u, x[r]);
-        return;
-    }
-    if (code == 0) {
-        if (all) gm_dispatch_j<0, true>(j, g, x); else gm_dispatch_j<0, false>(j, g, x);
-    } else if (code == 1) {
-        if (all) gm_dispatch_j<1, true>(j, g, x); else gm_dispatch_j<1, false>(j, g, x);
-    } else {
-        if (all) gm_dispatch_j<2, true>(j, g, x); else gm_dispatch_j<2, false>(j, g, x);
-    }
-}
-
-// One register group over the tile s (complex64). hdr is the OP_GROUP header, members follow it.
-__device__ __forceinline__ void group_run_c64(float2* s, uint32_t tsize, uint64_t base, const TileOp* hdr) {
-    const int cnt = hdr->k;
-    uint32_t goff[8], seg[5];
-#pragma unroll
-    for (int j = 0; j < 8; j++) goff[j] = hdr->off[j];
-#pragma unroll
-    for (int j = 0; j < 5; j++) seg[j] = hdr->seg[j];
-    const int npos = hdr->npos;
-    const uint32_t ng = tsize >> 3;
-    for (uint32_t p0 = threadIdx.x; p0 < ng; p0 += 2 * kTileThreads) {
-        const bool two = p0 + kTileThreads < ng;
-        const uint32_t b0 = tuple_index(p0, npos, seg, hdr->pos, 0u);
-        const uint32_t b1 = two ? tuple_index(p0 + kTileThreads, npos, seg, hdr->pos, 0u) : b0;
-        float2 x0[8], x1[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            x0[j] = s[b0 + goff[j]];
-            x1[j] = s[b1 + goff[j]];
-        }
-        for (int mi = 1; mi <= cnt; mi++) {
-            const TileOp& m = hdr[mi];
-            if ((base & m.omask) != m.oval) continue;
-            GMember g;
-#pragma unroll
-            for (int i = 0; i < 8; i++) g.u[i] = m.mf[i];
-            g.fm = m.gfin_mask;
-            g.fv = m.gfin_val;
-            g.pf0 = m.pf[0];
-            g.pf1 = m.pf[1];
-            g.s0 = m.offsrc[0] != 0;
-            g.s1 = m.offsrc[1] != 0;
-            const int code = m.gcode, j = m.gj;
-            const uint32_t om = m.gfout_mask, ov = m.gfout_val;
-            if ((b0 & om) == ov) gm_dispatch(code, j, g, x0);
-            if (two && (b1 & om) == ov) gm_dispatch(code, j, g, x1);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            s[b0 + goff[j]] = x0[j];
-            if (two) s[b1 + goff[j]] = x1[j];
-        }
-    }
 }
 
 // ---- fused 5-qubit blocks on the tensor cores (complex64 tiles, 3xTF32)
@@ -463,46 +349,6 @@ __device__ __forceinline__ void block_apply(float* sf, uint32_t tsize, const Til
     }
 }
 
-// ---- TMA bulk copies and mbarriers
-__device__ __forceinline__ uint32_t saddr(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(saddr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Wait for the phase of `parity` to complete, at most ~2 s of SM clocks.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > 4000000000LL) return false;
-    return true;
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     saddr(dst)),
-                 "l"(src), "r"(bytes), "r"(saddr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(saddr(src)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
 // Element type of the state in global memory (the tile buffer holds it while a copy is in flight).
 template <int REP>
 struct GlobElem {
@@ -528,12 +374,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t tsize = 1u << sa.T;
     E* bufs = reinterpret_cast<E*>(smem_raw);
-    const int nrows = 1 << sa.H;
-    uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem_raw + 2 * (sizeof(E) << sa.T));
-    uint64_t* mbar = rowoff + nrows;
-    TileOp* sops = reinterpret_cast<TileOp*>(mbar + 2);
-    __shared__ int s_abort;
+    const int nrows = 1 << sa.RH, nbuf = sa.nbuf;
     const int nops = sa.op_end - sa.op_begin;
+    // [tile buffers][nbuf mbarriers, padded to 32 bytes][ops (16-byte aligned)][row offsets]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + size_t(nbuf) * (sizeof(E) << sa.T));
+    TileOp* sops = reinterpret_cast<TileOp*>(mbar + 4);
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sops + nops);
+    __shared__ int s_abort;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
         uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
@@ -542,20 +389,19 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
     }
     for (int r = threadIdx.x; r < nrows; r += kTileThreads) {
         uint64_t o = 0;
-        for (int b = 0; b < sa.H; b++)
-            if (r >> b & 1) o |= 1ull << sa.high[b];
+        for (int b = 0; b < sa.RH; b++)
+            if (r >> b & 1) o |= 1ull << sa.rhigh[b];
         rowoff[r] = o;
     }
     if (threadIdx.x == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int b = 0; b < nbuf; b++) mbar_init(&mbar[b], 1);
         fence_mbar_init();
         s_abort = 0;
     }
     __syncthreads();
     const uint64_t first = blockIdx.x;
     const uint64_t nmy = (ntiles > first) ? (ntiles - 1 - first) / gridDim.x + 1 : 0;
-    const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.L;
+    const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.RL;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GE* gstate = static_cast<GE*>(state);
     auto issue_load = [&](uint64_t i, int b) {  // warp 0 only
@@ -563,20 +409,27 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
         if (lane == 0) mbar_expect_tx(&mbar[b], row_bytes * uint32_t(nrows));
         __syncwarp();
         for (int r = lane; r < nrows; r += 32)
-            bulk_load(bufs + size_t(b) * tsize + (size_t(r) << sa.L), gstate + tb + rowoff[r], row_bytes, &mbar[b]);
+            bulk_load(bufs + size_t(b) * tsize + (size_t(r) << sa.RL), gstate + tb + rowoff[r], row_bytes, &mbar[b]);
     };
     if (warp == 0 && nmy > 0) issue_load(0, 0);
     uint64_t it = 0;
+    int bsel = 0;          // buffer of tile it
+    uint32_t phase = 0;    // bit b: parity of buffer b's next completion
     for (; it < nmy; it++) {
-        const int bsel = int(it & 1);
         E* s = bufs + size_t(bsel) * tsize;
         const uint64_t base = expand_index(first + it * gridDim.x, sa.outer);
         if (warp == 0 && it + 1 < nmy) {
-            bulk_wait_read_all();  // the other buffer's previous store has read shared memory
+            // Tile it + 1 reuses the buffer of tile it + 1 - nbuf, whose stores were committed
+            // nbuf - 1 groups ago: wait until those have read shared memory.
+            if (nbuf == 3)
+                bulk_wait_read<1>();
+            else
+                bulk_wait_read<0>();
             __syncwarp();
-            issue_load(it + 1, bsel ^ 1);
+            issue_load(it + 1, bsel + 1 == nbuf ? 0 : bsel + 1);
         }
-        if (!mbar_wait_bounded(&mbar[bsel], uint32_t((it >> 1) & 1))) atomicOr(&s_abort, 1);
+        if (!mbar_wait_bounded(&mbar[bsel], (phase >> bsel) & 1u)) atomicOr(&s_abort, 1);
+        phase ^= 1u << bsel;
         __syncthreads();
         if (s_abort) break;
         if constexpr (REP == 2) {  // split the loaded doubles into double-float pairs, in place
@@ -602,8 +455,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
             if (BLK) {
                 if constexpr (REP == 3 && BLK)
                     if (kind == OP_BLOCK) block_apply(reinterpret_cast<float*>(s), tsize, op, bfrag);
-            } else if (REP == 3 && kind == OP_GROUP) {
-                if constexpr (REP == 3 && !BLK) group_run_c64(reinterpret_cast<float2*>(s), tsize, base, &sops[o]);
+            } else if (REP == 3 && kind == OP_PASS) {
+                if constexpr (REP == 3 && !BLK) pass_run_c64(reinterpret_cast<float2*>(s), tsize, base, &sops[o]);
                 o += op.k;
             } else if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
                 const uint32_t tb = op.off[1];
@@ -645,14 +498,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
         __syncthreads();
         if (warp == 0) {
             for (int r = lane; r < nrows; r += 32)
-                bulk_store(gstate + base + rowoff[r], s + (size_t(r) << sa.L), row_bytes);
+                bulk_store(gstate + base + rowoff[r], s + (size_t(r) << sa.RL), row_bytes);
             bulk_commit();
         }
+        bsel = bsel + 1 == nbuf ? 0 : bsel + 1;
     }
     if (warp == 0) bulk_wait_all();
     if (s_abort && threadIdx.x == 0) {
         atomicExch(err, 1);
-        if (it + 1 < nmy) mbar_wait_bounded(&mbar[int((it + 1) & 1)], uint32_t(((it + 1) >> 1) & 1));
+        // the load of tile it + 1 may still be in flight: wait for it (bounded) before exiting
+        const int nb = bsel + 1 == nbuf ? 0 : bsel + 1;
+        if (it + 1 < nmy) mbar_wait_bounded(&mbar[nb], (phase >> nb) & 1u);
     }
 }
 
@@ -679,15 +535,28 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     sa.outer.npos = int(qpos.size());
     for (size_t i = 0; i < qpos.size(); i++) sa.outer.pos[i] = uint8_t(qpos[i]);
     sa.outer.fixval = 0;
-    for (int b = 0; b < sa.H; b++) sa.high[b] = uint8_t(st.high[b]);
-    const size_t smem = 2 * (sizeof(E) << st.T) + (sizeof(uint64_t) << sa.H) + 2 * sizeof(uint64_t) +
-                        sizeof(TileOp) * size_t(op_end - op_begin);
+    // Copy rows: high qubits L, L + 1, ... continue the contiguous low run.
+    int run = 0;
+    while (run < sa.H && st.high[run] == st.L + run) run++;
+    sa.RL = st.L + run;
+    sa.RH = sa.H - run;
+    for (int b = 0; b < sa.RH; b++) sa.rhigh[b] = uint8_t(st.high[run + b]);
+    const size_t tile_bytes = sizeof(E) << st.T;
+    const size_t fixed = 4 * sizeof(uint64_t) + sizeof(TileOp) * size_t(op_end - op_begin) +
+                         (sizeof(uint64_t) << sa.RH);
+    sa.nbuf = (3 * tile_bytes + fixed <= 110 * 1024) ? 3 : 2;  // three buffers where two blocks still fit an SM
+    const size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_tile<REP, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
     }
     const uint64_t ntiles = 1ull << (n - st.T);
-    const int per_sm = std::max(1, std::min(8, int((220 * 1024) / smem)));
+    // One wave exactly: every CTA walks the same number of tiles, so a grid larger than what is
+    // resident would leave a second, partly empty wave.
+    int per_sm = 0;
+    cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<REP, BLK>, kTileThreads, smem);
+    if (oe != cudaSuccess) return oe;
+    per_sm = std::max(1, per_sm);
     const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * per_sm);
     k_tile<REP, BLK><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, dfrag, derr);
     cudaError_t e = cudaGetLastError();
@@ -713,12 +582,15 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
             if (!df64_range_ok(op)) rep = 1;  // entries outside double-float range: FP64 FMA instead
     std::vector<TileOp> host;
     std::vector<int> first(stages.size(), 0);
+    std::vector<char> passes(stages.size(), 0);
     for (size_t i = 0; i < stages.size(); i++) {
         first[i] = int(host.size());
         if (!stages[i].tiled) continue;
-        // Register groups pay off where shared-memory passes dominate (complex64); the
+        // Register passes pay off where shared-memory traffic dominates (complex64); the
         // FP64 and double-float tiles are arithmetic-bound and keep one pass per gate.
-        for (const TileOp& t : stage_program(ops, stages[i], rep == 3)) host.push_back(t);
+        const std::vector<TileOp> prog = stage_program(ops, stages[i], rep == 3);
+        passes[i] = rep == 3 && pass_only(prog);
+        for (const TileOp& t : prog) host.push_back(t);
     }
     // One allocation: the op table, then an error flag the tile kernels raise when a bounded wait gives up.
     TileOp* dops = nullptr;
@@ -765,6 +637,8 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
             default:
                 if (dfrag)
                     e = launch_tile<3, true>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
+                else if (passes[i])
+                    e = launch_pass(state, n, st, b, e2, dops, derr, s, sms);
                 else
                     e = launch_tile<3, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
                 break;

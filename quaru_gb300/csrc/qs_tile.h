@@ -17,13 +17,40 @@
 namespace qs {
 
 constexpr int kTileMaxHigh = 8;
-constexpr int kGroupBits = 3;          // register-group width: 8 amplitudes per thread
-constexpr uint8_t OP_GROUP = 10;       // TileOp kind of a register-group header
+constexpr int kPassBits = 4;           // register bits of a pass: 16 amplitudes per thread
+constexpr int kLaneBits = 4;           // tile bits 0..3 live on the lanes of a warp during a pass
+constexpr int kPassMinT = 9;           // passes need whole warps of tuples: 2^(T-4) >= 32
+constexpr uint8_t OP_PASS = 10;        // TileOp kind of a register-pass header
+
+// A gate inside a register pass (complex64 tiles). The pass holds 16 amplitudes per thread: the
+// register bits R (4 tile bits >= 4, chosen per pass) index the thread's registers, tile bits 0..3
+// are lane bits 0..3 of the warp, the remaining tile bits select the thread's tuple.
+//
+// Codes of a k = 1 gate: dense complex 2x2, dense real 2x2, swap (the rows exchanged: X, CNOT),
+// swap with phases (Y), two-row phase (RZ); a k = 0 gate is a phase on one row (Z, S, phase, CZ).
+enum PassCode : uint32_t { PC_DENSE = 0, PC_REAL = 1, PC_SWAP = 2, PC_SWAPPH = 3, PC_DIAG2 = 4 };
+// Variant ids (PassMember::ctl bits 0-7): one dispatch per member, the kernel decodes nothing else.
+//   register gate, code c, register bit J, no register controls a:   c * 8 + J * 2 + a          0..39
+//   swap on register bit J controlled by register bit C (value 1):    40 + J * 4 + C             40..55
+//   dense gates on the register bits of mask M (2..4 gates, J order): 56 + M                    56..71
+//   lane gate, code c, no register controls a, no tuple controls n:   72 + c * 4 + a * 2 + n     72..91
+//   k = 0 phase, no register controls a:                              92 + a                     92..93
+constexpr uint32_t kPvSwapC = 40, kPvMulti = 56, kPvLane = 72, kPvPhase = 92;
+struct alignas(16) PassMember {
+    float u[8];     // dense: row-major 2x2 complex; real: m00, m01, m10, m11; swap with phases and
+                    // two-row phase: factor of row 0 (u[0..1]) and row 1 (u[2..3]); k = 0: u[0..1]
+    uint32_t ctl;   // variant id (bits 0-7) | entries it consumes - 1 (8-9) | lane bit (10-11) |
+                    // controls outside the tile (12) | controls on tuple or lane bits (13)
+    uint32_t fmv;   // register controls: mask (bits 0-3), values (4-7)
+    uint32_t om;    // controls on tuple and lane bits (tile-local), compared with the tuple's base index
+    uint32_t ov;
+};
 
 // Gate as the tile kernel sees it (local bit numbering inside the tile).
-struct TileOp {
+struct alignas(16) TileOp {
+    PassMember pm;    // register-pass member fields (valid when the op follows an OP_PASS header)
     uint8_t kind;     // OpKind
-    uint8_t k;        // sub-operation arity (<= 3)
+    uint8_t k;        // sub-operation arity (<= 3); OP_PASS: number of members
     uint8_t tb[3];    // local bit of sub-operation target j
     uint8_t npos;     // number of sorted local positions below
     uint8_t pos[16];  // sorted local bits of targets and local fixed bits (for tuple expansion)
@@ -38,15 +65,7 @@ struct TileOp {
     float dfh[16];    // dense 1q double-float coefficients (see Dense1Args)
     float dfl[16];
     float mf[16];     // m rounded to float (complex64 registers)
-    // Register-group member fields (valid when the op follows an OP_GROUP header):
-    uint8_t gj;          // group-local target bit (0..2)
-    uint8_t gfin_mask;   // fixed bits inside the group (group-local)
-    uint8_t gfin_val;
-    uint8_t gcode;       // 0 dense, 1 dense real, 2 monomial k = 1, 3 phase on a fixed subspace (k = 0)
-    uint32_t gfout_mask; // fixed bits inside the tile but outside the group (tile-local)
-    uint32_t gfout_val;
     uint32_t bidx;       // OP_BLOCK: offset of the block's B fragments (float4 units)
-    uint32_t pad2_;
 };
 
 // Tensor-core fragments of one fused 5-qubit block: [n-tile 8][k-step 8][lane 32] float4
@@ -72,10 +91,18 @@ std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, 
 // Device image of one op inside `stage`.
 TileOp make_tile_op(const OpDesc& op, const TileStage& stage);
 
-// The device program of one stage: its ops, with runs of 1-qubit gates whose
-// targets span at most kGroupBits tile bits gathered behind OP_GROUP headers.
-// Gate order is unchanged.
-std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& stage, bool groups);
+// The device program of one stage: its ops in order, or (passes = true, complex64 tiles with
+// T >= kPassMinT) runs of k <= 1 gates scheduled into register passes behind OP_PASS headers.
+// Pass scheduling moves a gate only past gates that share no qubit with it.
+std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& stage, bool passes);
+
+// Whether a stage program (from stage_program) consists of register passes only.
+bool pass_only(const std::vector<TileOp>& prog);
+
+// Launch the warp-specialised complex64 pass kernel for one pass-only stage whose program is
+// dops[op_begin, op_end).
+cudaError_t launch_pass(void* state, int n, const TileStage& st, int op_begin, int op_end, const TileOp* dops,
+                        int* derr, cudaStream_t s, int sms);
 
 // Run stages on the device; ops are the host descriptors.
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,

@@ -5,9 +5,11 @@
 //
 // stdin (little-endian): n, T, L (int32); m (int32); per gate: k (int32),
 // k targets (int32), 2^k x 2^k complex (2*4^k doubles); then 2^n complex
-// amplitudes. stdout: 2^n complex amplitudes, then the number of stages.
+// amplitudes. stdout: 2^n complex amplitudes, the number of stages, the number of register passes.
 #include <algorithm>
+#include <array>
 #include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -44,37 +46,115 @@ uint64_t expand(uint64_t t, const std::vector<int>& pos) {
     return t;
 }
 
-// One k <= 1 member op of a register group applied to the 8 registers x.
-void group_apply(const qs::TileOp& m, C (&x)[8]) {
-    const int fm = m.gfin_mask, fv = m.gfin_val;
-    auto mono_row = [&](int r, C src) -> C {
-        return (m.pf[r] == 255) ? cmul(m.m[2 * r], m.m[2 * r + 1], src) : pf(src, m.pf[r]);
-    };
-    if (m.k == 0) {
-        for (int r = 0; r < 8; r++)
-            if ((r & fm) == fv && m.pf[0] != 4) x[r] = mono_row(0, x[r]);
-        return;
+// One register pass (OP_PASS header at tops[oi]) over the tile s, decoding the kernel's variant ids
+// (qs_tile.h) independently of the kernel: tuple p holds 16 registers at base(p) | off[j]; tile bits
+// 0..3 are lane bits, so a gate on lane bit t pairs tuple p with tuple p ^ (1 << t). Arithmetic uses
+// the entries' double coefficients (TileOp::m), in the layouts the variants read as floats.
+void run_pass(std::vector<C>& s, uint32_t tsize, uint64_t tile_base, const std::vector<qs::TileOp>& tops,
+              size_t oi) {
+    const qs::TileOp& h = tops[oi];
+    const uint32_t ntup = tsize >> 4;
+    std::vector<uint32_t> base(ntup);
+    std::vector<std::array<C, 16>> X(ntup);
+    auto off = [&](int j) { return j < 8 ? h.off[j] : h.offsrc[j - 8]; };
+    for (int j = 0; j < 16; j++) {  // the header's offsets must deposit j on the register bits
+        uint32_t o = 0;
+        for (int b = 0; b < 4; b++)
+            if (j >> b & 1) o |= 1u << h.pos[b];
+        if (off(j) != o) std::abort();
     }
-    const int j = m.gj;
-    for (int a = 0; a < 8; a++) {
-        if (a >> j & 1) continue;
-        if ((a & fm) != fv) continue;
-        const int b = a | (1 << j);
-        if (m.kind == qs::OP_DENSE || m.kind == qs::OP_DENSE_REAL) {
-            C y0 = cadd(cmul(m.m[0], m.m[1], x[a]), cmul(m.m[2], m.m[3], x[b]));
-            C y1 = cadd(cmul(m.m[4], m.m[5], x[a]), cmul(m.m[6], m.m[7], x[b]));
-            x[a] = y0;
-            x[b] = y1;
-        } else {
-            const C s0 = m.offsrc[0] ? x[b] : x[a];
-            const C s1 = m.offsrc[1] ? x[b] : x[a];
-            if (m.pf[0] != 4) x[a] = mono_row(0, s0);
-            if (m.pf[1] != 4) x[b] = mono_row(1, s1);
+    for (uint32_t p = 0; p < ntup; p++) {
+        uint32_t b0 = p & h.seg[0];
+        for (int j = 1; j <= 4; j++) b0 |= (p << j) & h.seg[j];
+        base[p] = b0;
+        for (int j = 0; j < 16; j++) X[p][j] = s[b0 | off(j)];
+    }
+    auto dense = [&](const double* m, C x0, C x1, int row) {
+        return cadd(cmul(m[4 * row], m[4 * row + 1], x0), cmul(m[4 * row + 2], m[4 * row + 3], x1));
+    };
+    // register gate of `code` on bit J with coefficients m, where (a & fm) == fv
+    auto reg_gate = [&](std::array<C, 16>& x, int code, int J, const double* m, int fm, int fv) {
+        for (int a = 0; a < 16; a++) {
+            if (a >> J & 1) continue;
+            if ((a & fm) != fv) continue;
+            const int b = a | (1 << J);
+            const C x0 = x[a], x1 = x[b];
+            if (code == qs::PC_DENSE) {
+                x[a] = dense(m, x0, x1, 0);
+                x[b] = dense(m, x0, x1, 1);
+            } else if (code == qs::PC_REAL) {
+                x[a] = cadd(cmul(m[0], 0, x0), cmul(m[2], 0, x1));
+                x[b] = cadd(cmul(m[4], 0, x0), cmul(m[6], 0, x1));
+            } else if (code == qs::PC_SWAP) {
+                x[a] = x1;
+                x[b] = x0;
+            } else if (code == qs::PC_SWAPPH) {
+                x[a] = cmul(m[0], m[1], x1);
+                x[b] = cmul(m[2], m[3], x0);
+            } else {
+                x[a] = cmul(m[0], m[1], x0);
+                x[b] = cmul(m[2], m[3], x1);
+            }
+        }
+    };
+    for (int mi = 1; mi <= h.k;) {
+        const qs::TileOp& m = tops[oi + mi];
+        const qs::PassMember& g = m.pm;
+        const uint32_t vid = g.ctl & 255u;
+        const int adv = int((g.ctl >> 8) & 3u) + 1;
+        mi += adv;
+        if ((g.ctl & (1u << 12)) && (tile_base & m.omask) != m.oval) continue;
+        const bool cond = g.ctl & (1u << 13);
+        int fm = g.fmv & 15, fv = (g.fmv >> 4) & 15;
+        if (vid >= qs::kPvLane && vid < qs::kPvPhase) {
+            const uint32_t c = vid - qs::kPvLane;
+            const int code = int(c / 4), t = int((g.ctl >> 10) & 3u);
+            if (c & 2) fm = fv = 0;
+            const bool nocond = c & 1;
+            auto Y = X;
+            for (uint32_t p = 0; p < ntup; p++) {
+                if (!nocond && (base[p] & g.om) != g.ov) continue;
+                const uint32_t q = p ^ (1u << t);
+                const int v = (base[p] >> t) & 1;
+                for (int j = 0; j < 16; j++) {
+                    if ((j & fm) != fv) continue;
+                    const C x0 = v ? X[q][j] : X[p][j], x1 = v ? X[p][j] : X[q][j];
+                    std::array<C, 16> pair{};
+                    pair[0] = x0;
+                    pair[1] = x1;
+                    reg_gate(pair, code, 0, m.m, 0, 0);
+                    Y[p][j] = pair[v];
+                }
+            }
+            X.swap(Y);
+            continue;
+        }
+        for (uint32_t p = 0; p < ntup; p++) {
+            if (cond && (base[p] & g.om) != g.ov) continue;
+            auto& x = X[p];
+            if (vid < qs::kPvSwapC) {
+                if (vid & 1u) fm = fv = 0;
+                reg_gate(x, int(vid / 8), int((vid % 8) / 2), m.m, fm, fv);
+            } else if (vid < qs::kPvMulti) {
+                const int J = int((vid - qs::kPvSwapC) / 4), Cb = int((vid - qs::kPvSwapC) % 4);
+                reg_gate(x, qs::PC_SWAP, J, m.m, 1 << Cb, 1 << Cb);
+            } else if (vid < qs::kPvLane) {
+                const uint32_t M = vid - qs::kPvMulti;
+                int e = 0;
+                for (int J = 0; J < 4; J++)
+                    if (M >> J & 1u) reg_gate(x, qs::PC_DENSE, J, tops[oi + (mi - adv) + e++].m, 0, 0);
+            } else {
+                if (vid & 1u) fm = fv = 0;
+                for (int j = 0; j < 16; j++)
+                    if ((j & fm) == fv) x[j] = cmul(m.m[0], m.m[1], x[j]);
+            }
         }
     }
+    for (uint32_t p = 0; p < ntup; p++)
+        for (int j = 0; j < 16; j++) s[base[p] | off(j)] = X[p][j];
 }
 
-// Emulates k_tile<0> (the exact representation) for one stage.
+// Emulates k_tile for one stage (k_tile<0>'s arithmetic for the per-gate ops).
 void run_stage(std::vector<C>& st, int n, const qs::TileStage& stage, const std::vector<qs::TileOp>& tops) {
     const int T = stage.T, L = stage.L, H = int(stage.high.size());
     std::vector<int> qpos;
@@ -97,20 +177,8 @@ void run_stage(std::vector<C>& st, int n, const qs::TileStage& stage, const std:
             const qs::TileOp& op = tops[oi];
             if ((base & op.omask) != op.oval) continue;
             const uint32_t ntup = tsize >> op.npos;
-            if (op.kind == qs::OP_GROUP) {
-                for (uint32_t p = 0; p < ntup; p++) {
-                    uint32_t b0 = p & op.seg[0];
-                    for (int j = 1; j <= op.npos; j++) b0 |= (p << j) & op.seg[j];
-                    C x[8];
-                    for (int j = 0; j < 8; j++) x[j] = s[b0 + op.off[j]];
-                    for (int mi = 1; mi <= op.k; mi++) {
-                        const qs::TileOp& m = tops[oi + mi];
-                        if ((base & m.omask) != m.oval) continue;
-                        if ((b0 & m.gfout_mask) != m.gfout_val) continue;
-                        group_apply(m, x);
-                    }
-                    for (int j = 0; j < 8; j++) s[b0 + op.off[j]] = x[j];
-                }
+            if (op.kind == qs::OP_PASS) {
+                run_pass(s, tsize, base, tops, oi);
                 oi += op.k;
                 continue;
             }
@@ -153,7 +221,10 @@ bool rd(V* v, size_t count) {
 
 }  // namespace
 
-int main() {
+int main(int argc, char** argv) {
+    // argv[1] == "pass": plan as for complex64 (commuting gates may reorder) with register passes;
+    // otherwise the exact-order plan with one shared-memory pass per gate.
+    const bool passes = argc > 1 && std::strcmp(argv[1], "pass") == 0;
     int32_t n, T, L, m;
     if (!rd(&n, 1) || !rd(&T, 1) || !rd(&L, 1) || !rd(&m, 1)) return 2;
     std::vector<qs::OpDesc> ops(m);
@@ -171,7 +242,8 @@ int main() {
     }
     std::vector<C> st(size_t(1) << n);
     if (!rd(reinterpret_cast<double*>(st.data()), 2 * st.size())) return 2;
-    const auto stages = qs::plan_tiles(ops, n, T, L, true);
+    const auto stages = qs::plan_tiles(ops, n, T, L, !passes);
+    int32_t npasses = 0;
     for (const auto& stage : stages) {
         if (!stage.tiled) {
             // single wide or dense gate: apply like the reference (sequential order suffices for
@@ -204,11 +276,13 @@ int main() {
             st.swap(out);
             continue;
         }
-        const std::vector<qs::TileOp> tops = qs::stage_program(ops, stage, true);
+        const std::vector<qs::TileOp> tops = qs::stage_program(ops, stage, passes);
+        for (const auto& t : tops) npasses += t.kind == qs::OP_PASS;
         run_stage(st, n, stage, tops);
     }
     fwrite(st.data(), sizeof(C), st.size(), stdout);
     int32_t ns = int32_t(stages.size());
     fwrite(&ns, sizeof(ns), 1, stdout);
+    fwrite(&npasses, sizeof(npasses), 1, stdout);
     return 0;
 }

@@ -33,17 +33,17 @@ def emulator():
     return EXE
 
 
-def run_emulator(exe, n, T, L, ops, state):
+def run_emulator(exe, n, T, L, ops, state, mode="exact"):
     buf = bytearray(struct.pack("<4i", n, T, L, len(ops)))
     for op in ops:
         t = list(op.targets)
         buf += struct.pack("<i", len(t)) + struct.pack(f"<{len(t)}i", *t)
         buf += np.ascontiguousarray(np.asarray(op.matrix, dtype=np.complex128)).tobytes()
     buf += np.ascontiguousarray(state, dtype=np.complex128).tobytes()
-    r = subprocess.run([str(exe)], input=bytes(buf), capture_output=True, check=True)
+    r = subprocess.run([str(exe), mode], input=bytes(buf), capture_output=True, check=True)
     out = np.frombuffer(r.stdout[: 16 << n], dtype=np.complex128)
-    stages = struct.unpack("<i", r.stdout[16 << n:])[0]
-    return out, stages
+    stages, passes = struct.unpack("<2i", r.stdout[16 << n:])
+    return (out, stages, passes) if mode == "pass" else (out, stages)
 
 
 def cases():
@@ -78,6 +78,25 @@ def test_planned_tiles_match_oracle(emulator, oracle_mod, T, L):
         assert stages < len(ops), name
         bad = np.nonzero(~((got.view(np.float64) == o.state.view(np.float64))))[0]
         assert bad.size == 0, f"{name}: {bad.size} values differ, first at {bad[:4]}"
+
+
+@pytest.mark.parametrize("T,L", [(12, 5), (9, 5), (10, 3), (13, 5)])
+def test_register_passes_match_oracle(emulator, oracle_mod, T, L):
+    """The complex64 stage program: gates scheduled into 16-register passes (lane-bit gates
+    through partner tuples), commuting gates reordered; equal to the oracle up to rounding."""
+    for name, n, ops in cases():
+        rng = np.random.default_rng(len(ops) + 7)
+        st = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        st /= np.linalg.norm(st)
+        o = oracle_mod.OracleRegister.from_int(n, 0)
+        o.state = st.copy()
+        o.apply_sequence([(g.matrix, g.targets) for g in ops])
+        got, stages, passes = run_emulator(emulator, n, min(T, n), min(L, n), ops, st, mode="pass")
+        assert stages < len(ops), name
+        if min(T, n) >= 9:
+            assert passes > 0, name
+        err = np.max(np.abs(got - o.state) / np.maximum(np.abs(o.state), 2.0 ** (-n / 2)))
+        assert err < 1e-12, f"{name}: relative error {err}"
 
 
 FUSE_SRC = ROOT / "tests" / "cpp" / "fuse_check.cpp"
