@@ -21,8 +21,8 @@
 
 namespace qs {
 
-constexpr int kPassCompute = 256;                 // compute threads (one tuple of 16 amplitudes each)
-constexpr int kPassThreads = kPassCompute + 32;   // plus the copy warp
+// NC compute threads (one tuple of 16 amplitudes each: 256 for 4096-amplitude tiles, 512 for 8192)
+// plus the copy warp.
 
 struct PassArgs {
     int T;
@@ -33,26 +33,28 @@ struct PassArgs {
     uint8_t rhigh[kTileMaxHigh];  // global qubit of row bit b
 };
 
+template <int NC>
 __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntiles,
                                                            const __grid_constant__ PassArgs pa,
                                                            const TileOp* __restrict__ ops, int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t tsize = 1u << pa.T;
     const int nbuf = pa.nbuf, nops = pa.op_end - pa.op_begin, nrows = 1 << pa.RH;
-    // [tile buffers][full[4]][done[4]][ops (16-byte aligned)][row offsets]
+    // [tile buffers][full[4]][done[4]][tile base of each buffer[4]][ops (16-byte aligned)][row offsets]
     float2* bufs = reinterpret_cast<float2*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + size_t(nbuf) * (sizeof(float2) << pa.T));
     uint64_t* done = full + 4;
-    TileOp* sops = reinterpret_cast<TileOp*>(done + 4);
+    uint64_t* tbase = done + 4;  // written by the copy warp before the load that completes full[b]
+    TileOp* sops = reinterpret_cast<TileOp*>(tbase + 4);
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(sops + nops);
     __shared__ volatile int s_abort;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + pa.op_begin);
         uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
         const int words = nops * int(sizeof(TileOp) / 4);
-        for (int w = threadIdx.x; w < words; w += kPassThreads) dst[w] = src[w];
+        for (int w = threadIdx.x; w < words; w += NC + 32) dst[w] = src[w];
     }
-    for (int r = threadIdx.x; r < nrows; r += kPassThreads) {
+    for (int r = threadIdx.x; r < nrows; r += NC + 32) {
         uint64_t o = 0;
         for (int b = 0; b < pa.RH; b++)
             if (r >> b & 1) o |= 1ull << pa.rhigh[b];
@@ -61,7 +63,7 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) {
             mbar_init(&full[b], 1);
-            mbar_init(&done[b], kPassCompute);
+            mbar_init(&done[b], NC);
         }
         fence_mbar_init();
         s_abort = 0;
@@ -71,12 +73,15 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
     const uint64_t nmy = (ntiles > first) ? (ntiles - 1 - first) / gridDim.x + 1 : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    if (warp == kPassCompute / 32) {
+    if (warp == NC / 32) {
         // ---------------------------------------------------------------- copy warp
         const uint32_t row_bytes = uint32_t(sizeof(float2)) << pa.RL;
         auto issue_load = [&](uint64_t i, int b) {
             const uint64_t tb = expand_index(first + i * gridDim.x, pa.outer);
-            if (lane == 0) mbar_expect_tx(&full[b], row_bytes * uint32_t(nrows));
+            if (lane == 0) {
+                tbase[b] = tb;  // released to the compute warps by the mbarrier's phase completion
+                mbar_expect_tx(&full[b], row_bytes * uint32_t(nrows));
+            }
             __syncwarp();
             for (int r = lane; r < nrows; r += 32)
                 bulk_load(bufs + size_t(b) * tsize + (size_t(r) << pa.RL), state + tb + rowoff[r], row_bytes,
@@ -127,17 +132,16 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
     int b = 0;
     for (uint64_t it = 0; it < nmy; it++) {
         if (!mbar_wait_bounded(&full[b], (fphase >> b) & 1u)) s_abort = 1;
-        named_sync(1, kPassCompute);  // every compute thread sees the same s_abort
+        named_sync(1, NC);  // every compute thread sees the same s_abort
         if (s_abort) {
             if (threadIdx.x == 0) atomicExch(err, 1);
             break;
         }
         fphase ^= 1u << b;
         float2* s = bufs + size_t(b) * tsize;
-        const uint64_t tile_base = expand_index(first + it * gridDim.x, pa.outer);
         for (int o = 0; o < nops; o += int(sops[o].k) + 1) {
-            if (o > 0) named_sync(1, kPassCompute);
-            pass_run_c64(s, tsize, tile_base, &sops[o]);
+            if (o > 0) named_sync(1, NC);
+            pass_run_c64<NC>(s, tsize, &tbase[b], &sops[o]);
         }
         fence_async_shared();  // this thread's writes, visible to the bulk stores
         mbar_arrive(&done[b]);
@@ -167,17 +171,23 @@ cudaError_t launch_pass(void* state, int n, const TileStage& st, int op_begin, i
     pa.outer.fixval = 0;
     const size_t tile_bytes = sizeof(float2) << st.T;
     const size_t fixed =
-        8 * sizeof(uint64_t) + sizeof(TileOp) * size_t(op_end - op_begin) + (sizeof(uint64_t) << pa.RH);
-    pa.nbuf = (3 * tile_bytes + fixed <= 110 * 1024) ? 3 : 2;  // three buffers where two blocks still fit an SM
+        12 * sizeof(uint64_t) + sizeof(TileOp) * size_t(op_end - op_begin) + (sizeof(uint64_t) << pa.RH);
+    // three buffers where two blocks still fit an SM (4096-amplitude tiles), or one block (8192)
+    pa.nbuf = (3 * tile_bytes + fixed <= (st.T >= 13 ? 220 : 110) * 1024) ? 3 : 2;
     const size_t smem = size_t(pa.nbuf) * tile_bytes + fixed;
-    cudaError_t e = cudaFuncSetAttribute(k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass, kPassThreads, smem);
-    if (e != cudaSuccess) return e;
     const uint64_t ntiles = 1ull << (n - st.T);
-    const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm)));
-    k_pass<<<int(grid), kPassThreads, smem, s>>>(static_cast<float2*>(state), ntiles, pa, dops, derr);
+    auto go = [&](auto kern, int nthreads) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nthreads, smem);
+        if (e != cudaSuccess) return e;
+        const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm)));
+        kern<<<int(grid), nthreads, smem, s>>>(static_cast<float2*>(state), ntiles, pa, dops, derr);
+        return cudaSuccess;
+    };
+    cudaError_t e = (st.T >= 13) ? go(k_pass<512>, 512 + 32) : go(k_pass<256>, 256 + 32);
+    if (e != cudaSuccess) return e;
     e = cudaGetLastError();
     if (e == cudaSuccess) note_launches(1);
     return e;

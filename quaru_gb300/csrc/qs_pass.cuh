@@ -90,17 +90,6 @@ __device__ __forceinline__ void pv_swapc(float2 (&x)[16]) {
     }
 }
 
-// Dense gates on the register bits of mask M, in increasing bit order; their coefficients are the
-// u of consecutive entries starting at m.
-template <int M>
-__device__ __forceinline__ void pv_multi(const TileOp* m, float2 (&x)[16]) {
-    int e = 0;
-    if (M & 1) pv_dense<0, true>(m[e++].pm.u, 0, 0, x);
-    if (M & 2) pv_dense<1, true>(m[e++].pm.u, 0, 0, x);
-    if (M & 4) pv_dense<2, true>(m[e++].pm.u, 0, 0, x);
-    if (M & 8) pv_dense<3, true>(m[e++].pm.u, 0, 0, x);
-}
-
 // Gate on lane bit t: every thread computes its own row from its amplitude and its partner's; all
 // lanes take part in the shuffles. NOCOND: no controls on tuple or lane bits (`on` is ignored).
 template <int CODE, bool ALL, bool NOCOND>
@@ -158,86 +147,111 @@ __device__ __forceinline__ void pv_phase(const float* u, int fm, int fv, float2 
     }
 }
 
-// Apply member m (its variant id in ctl) to the thread's registers.
+// Calls F<0..3>(...) by the two-bit field of v at `shift`, with bit tests (no jump table).
+#define QS_PV_J4(v, shift, CALL) \
+    if (((v) >> ((shift) + 1)) & 1u) {         \
+        if (((v) >> (shift)) & 1u) {           \
+            CALL(3);                            \
+        } else {                                \
+            CALL(2);                            \
+        }                                       \
+    } else {                                    \
+        if (((v) >> (shift)) & 1u) {           \
+            CALL(1);                            \
+        } else {                                \
+            CALL(0);                            \
+        }                                       \
+    }
+
+// Apply member m (its variant id in ctl) to the thread's registers. The dispatch is a shallow tree
+// of bit tests: a large switch costs about a hundred extra instructions per gate on sm_103a.
 __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t base, float2 (&x)[16]) {
     const PassMember& g = m->pm;
-    const uint32_t vid = ctl & 255u;
-    const bool cond = ctl & (1u << 13);
-    const bool on = !cond || (base & g.om) == g.ov;
-    if ((vid < kPvLane || vid >= kPvPhase) && !on) return;  // register and phase gates: controls fail
+    const uint32_t vid = ctl & 255u, cat = vid >> 4, low = vid & 15u;
+    if (cat == PV_DENSES) {  // 1..4 dense gates without controls, one entry each
+        int e = 0;
+        if (low & 1u) pv_dense<0, true>(m[e++].pm.u, 0, 0, x);
+        if (low & 2u) pv_dense<1, true>(m[e++].pm.u, 0, 0, x);
+        if (low & 4u) pv_dense<2, true>(m[e++].pm.u, 0, 0, x);
+        if (low & 8u) pv_dense<3, true>(m[e++].pm.u, 0, 0, x);
+        return;
+    }
+    const bool on = !(ctl & (1u << 13)) || (base & g.om) == g.ov;
     const int fm = g.fmv & 15, fv = (g.fmv >> 4) & 15;
-    switch (vid) {
-#define QS_PV_J(C, J, CALL_ALL, CALL_CTL) \
-    case C * 8 + J * 2:                   \
-        CALL_CTL;                         \
-        break;                            \
-    case C * 8 + J * 2 + 1:               \
-        CALL_ALL;                         \
-        break;
-#define QS_PV_CODE(C, FN)                                                                                     \
-    QS_PV_J(C, 0, (FN<0, true>(g.u, fm, fv, x)), (FN<0, false>(g.u, fm, fv, x)))                              \
-    QS_PV_J(C, 1, (FN<1, true>(g.u, fm, fv, x)), (FN<1, false>(g.u, fm, fv, x)))                              \
-    QS_PV_J(C, 2, (FN<2, true>(g.u, fm, fv, x)), (FN<2, false>(g.u, fm, fv, x)))                              \
-    QS_PV_J(C, 3, (FN<3, true>(g.u, fm, fv, x)), (FN<3, false>(g.u, fm, fv, x)))
-#define QS_PV_MONO(C)                                                                                          \
-    QS_PV_J(C, 0, (pv_mono<0, C, true>(g.u, fm, fv, x)), (pv_mono<0, C, false>(g.u, fm, fv, x)))               \
-    QS_PV_J(C, 1, (pv_mono<1, C, true>(g.u, fm, fv, x)), (pv_mono<1, C, false>(g.u, fm, fv, x)))               \
-    QS_PV_J(C, 2, (pv_mono<2, C, true>(g.u, fm, fv, x)), (pv_mono<2, C, false>(g.u, fm, fv, x)))               \
-    QS_PV_J(C, 3, (pv_mono<3, C, true>(g.u, fm, fv, x)), (pv_mono<3, C, false>(g.u, fm, fv, x)))
-        QS_PV_CODE(0, pv_dense)
-        QS_PV_CODE(1, pv_real)
-        QS_PV_MONO(2)
-        QS_PV_MONO(3)
-        QS_PV_MONO(4)
-#undef QS_PV_MONO
-#undef QS_PV_CODE
-#undef QS_PV_J
-#define QS_PV_SC(J, C)                 \
-    case kPvSwapC + J * 4 + C:         \
-        pv_swapc<J, C>(x);             \
-        break;
-        QS_PV_SC(0, 1) QS_PV_SC(0, 2) QS_PV_SC(0, 3)
-        QS_PV_SC(1, 0) QS_PV_SC(1, 2) QS_PV_SC(1, 3)
-        QS_PV_SC(2, 0) QS_PV_SC(2, 1) QS_PV_SC(2, 3)
-        QS_PV_SC(3, 0) QS_PV_SC(3, 1) QS_PV_SC(3, 2)
+    const bool all = low & 2u, nocond = low & 1u;
+    if (cat == PV_LDENSE || cat == PV_LSWAP) {  // lane gates: every lane takes part in the shuffles
+#define QS_PV_LANE(C)                                                          \
+    {                                                                          \
+        if (all) {                                                             \
+            if (nocond) pv_lane<C, true, true>(g, base, on, x);               \
+            else pv_lane<C, true, false>(g, base, on, x);                     \
+        } else {                                                               \
+            if (nocond) pv_lane<C, false, true>(g, base, on, x);              \
+            else pv_lane<C, false, false>(g, base, on, x);                    \
+        }                                                                      \
+    }
+        if (cat == PV_LDENSE) QS_PV_LANE(PC_DENSE) else QS_PV_LANE(PC_SWAP)
+        return;
+    }
+    if (!on) return;  // register and phase gates: this tuple fails the controls
+    if (cat == PV_SWAP) {
+#define QS_PV_SW(J) \
+    if (all) pv_mono<J, PC_SWAP, true>(g.u, fm, fv, x); else pv_mono<J, PC_SWAP, false>(g.u, fm, fv, x)
+        QS_PV_J4(low, 2, QS_PV_SW)
+#undef QS_PV_SW
+        return;
+    }
+    if (cat == PV_SWAPC) {
+#define QS_PV_SC(J)                                            \
+    {                                                          \
+        const uint32_t c = low & 3u;                           \
+        if (c == 0) pv_swapc<J, (J == 0 ? 1 : 0)>(x);          \
+        else if (c == 1) pv_swapc<J, (J == 1 ? 0 : 1)>(x);     \
+        else if (c == 2) pv_swapc<J, (J == 2 ? 0 : 2)>(x);     \
+        else pv_swapc<J, (J == 3 ? 0 : 3)>(x);                 \
+    }
+        QS_PV_J4(low, 2, QS_PV_SC)
 #undef QS_PV_SC
-#define QS_PV_M(M)             \
-    case kPvMulti + M:         \
-        pv_multi<M>(m, x);     \
-        break;
-        QS_PV_M(3) QS_PV_M(5) QS_PV_M(6) QS_PV_M(7) QS_PV_M(9) QS_PV_M(10) QS_PV_M(11)
-        QS_PV_M(12) QS_PV_M(13) QS_PV_M(14) QS_PV_M(15)
-#undef QS_PV_M
-#define QS_PV_L(C)                                        \
-    case kPvLane + C * 4 + 0:                             \
-        pv_lane<C, false, false>(g, base, on, x);         \
-        break;                                            \
-    case kPvLane + C * 4 + 1:                             \
-        pv_lane<C, false, true>(g, base, on, x);          \
-        break;                                            \
-    case kPvLane + C * 4 + 2:                             \
-        pv_lane<C, true, false>(g, base, on, x);          \
-        break;                                            \
-    case kPvLane + C * 4 + 3:                             \
-        pv_lane<C, true, true>(g, base, on, x);           \
-        break;
-        QS_PV_L(0) QS_PV_L(1) QS_PV_L(2) QS_PV_L(3) QS_PV_L(4)
-#undef QS_PV_L
-        case kPvPhase:
-            pv_phase<false>(g.u, fm, fv, x);
-            break;
-        case kPvPhase + 1:
-            pv_phase<true>(g.u, fm, fv, x);
-            break;
-        default:
-            break;
+        return;
+    }
+    if (cat == PV_PHASE) {
+        if (all) pv_phase<true>(g.u, fm, fv, x); else pv_phase<false>(g.u, fm, fv, x);
+        return;
+    }
+    // the rarer codes
+    if (cat >= PV_LREAL) {
+        if (cat == PV_LREAL) QS_PV_LANE(PC_REAL) else if (cat == PV_LSWAPPH) QS_PV_LANE(PC_SWAPPH) else QS_PV_LANE(PC_DIAG2)
+        return;
+    }
+#undef QS_PV_LANE
+    if (cat == PV_DENSE) {
+#define QS_PV_D(J) if (all) pv_dense<J, true>(g.u, fm, fv, x); else pv_dense<J, false>(g.u, fm, fv, x)
+        QS_PV_J4(low, 2, QS_PV_D)
+#undef QS_PV_D
+    } else if (cat == PV_REAL) {
+#define QS_PV_R(J) if (all) pv_real<J, true>(g.u, fm, fv, x); else pv_real<J, false>(g.u, fm, fv, x)
+        QS_PV_J4(low, 2, QS_PV_R)
+#undef QS_PV_R
+    } else if (cat == PV_SWAPPH) {
+#define QS_PV_P(J) \
+    if (all) pv_mono<J, PC_SWAPPH, true>(g.u, fm, fv, x); else pv_mono<J, PC_SWAPPH, false>(g.u, fm, fv, x)
+        QS_PV_J4(low, 2, QS_PV_P)
+#undef QS_PV_P
+    } else {
+#define QS_PV_G(J) \
+    if (all) pv_mono<J, PC_DIAG2, true>(g.u, fm, fv, x); else pv_mono<J, PC_DIAG2, false>(g.u, fm, fv, x)
+        QS_PV_J4(low, 2, QS_PV_G)
+#undef QS_PV_G
     }
 }
+#undef QS_PV_J4
 
-// One register pass over the tile s. hdr is the OP_PASS header (its off[] and offsrc[] hold the 16
-// register offsets), its member entries follow it; threads 0..255 take one tuple each per 4096
-// amplitudes (2^(T-4) tuples, a multiple of 32).
-__device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, uint64_t tile_base, const TileOp* hdr) {
+// One register pass over the tile s whose base amplitude index is *tile_base (read only for gates
+// with controls outside the tile). hdr is the OP_PASS header (its off[] and offsrc[] hold the 16
+// register offsets), its member entries follow it; threads 0..NT-1 take the 2^(T-4) tuples (a
+// multiple of 32) in turn.
+template <int NT = 256>
+__device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, const uint64_t* tile_base, const TileOp* hdr) {
     const int cnt = hdr->k;
     const uint32_t seg0 = hdr->seg[0], seg1 = hdr->seg[1], seg2 = hdr->seg[2], seg3 = hdr->seg[3],
                    seg4 = hdr->seg[4];
@@ -245,7 +259,7 @@ __device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, uint64_t
     // so they hold no registers while the members run
     auto off = [&](int j) -> uint32_t { return j < 8 ? hdr->off[j] : hdr->offsrc[j - 8]; };
     const uint32_t ntup = tsize >> kPassBits;
-    for (uint32_t p = threadIdx.x; p < ntup; p += 256) {
+    for (uint32_t p = threadIdx.x; p < ntup; p += NT) {
         const uint32_t base = (p & seg0) | ((p << 1) & seg1) | ((p << 2) & seg2) | ((p << 3) & seg3) |
                               ((p << 4) & seg4);
         float2* sb = s + base;
@@ -255,7 +269,7 @@ __device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, uint64_t
         for (int mi = 1; mi <= cnt;) {
             const TileOp* m = hdr + mi;
             const uint32_t ctl = m->pm.ctl;
-            if (!(ctl & (1u << 12)) || (tile_base & m->omask) == m->oval) pv_apply(m, ctl, base, x);
+            if (!(ctl & (1u << 12)) || (*tile_base & m->omask) == m->oval) pv_apply(m, ctl, base, x);
             mi += int((ctl >> 8) & 3u) + 1;
         }
 #pragma unroll

@@ -260,7 +260,7 @@ static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
     const uint32_t all = fm == 0 ? 1u : 0u, nocond = pm.om == 0 ? 1u : 0u;
     uint32_t vid, lane = 0;
     if (t.k == 0) {  // phase on the rows matching the controls
-        vid = kPvPhase + all;
+        vid = (PV_PHASE << 4) | (all << 1);
         pm.u[0] = float(t.m[0]);
         pm.u[1] = float(t.m[1]);
     } else {
@@ -285,14 +285,20 @@ static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
         }
         const int lb = t.tb[0];
         if (lb < kLaneBits) {
+            static const uint32_t lane_cat[5] = {PV_LDENSE, PV_LREAL, PV_LSWAP, PV_LSWAPPH, PV_LDIAG2};
             lane = uint32_t(lb);
-            vid = kPvLane + code * 4 + all * 2 + nocond;
+            vid = (lane_cat[code] << 4) | (all << 1) | nocond;
         } else {
             const uint32_t J = uint32_t(rix(lb));
-            vid = code * 8 + J * 2 + all;
-            // CNOT with its control on another register bit: a fixed register permutation
-            if (code == PC_SWAP && __builtin_popcount(fm) == 1 && fv == fm)
-                vid = kPvSwapC + J * 4 + uint32_t(__builtin_ctz(fm));
+            const bool plain = all && nocond && !t.omask;
+            if (code == PC_DENSE && plain)
+                vid = (PV_DENSES << 4) | (1u << J);
+            else if (code == PC_SWAP && fm && __builtin_popcount(fm) == 1 && fv == fm && nocond)
+                vid = (PV_SWAPC << 4) | (J << 2) | uint32_t(__builtin_ctz(fm));  // CNOT inside the registers
+            else {
+                static const uint32_t reg_cat[5] = {PV_DENSE, PV_REAL, PV_SWAP, PV_SWAPPH, PV_DIAG2};
+                vid = (reg_cat[code] << 4) | (J << 2) | (all << 1);
+            }
         }
     }
     pm.ctl = vid | (lane << 10) | (t.omask ? (1u << 12) : 0u) | (pm.om ? (1u << 13) : 0u);
@@ -302,8 +308,8 @@ static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
 // Whether member entry e is a single dense gate on a register bit with no controls of any kind.
 static bool plain_dense(const TileOp& e, int* J) {
     const uint32_t vid = e.pm.ctl & 255u;
-    if (vid >= 8 || !(vid & 1u) || (e.pm.ctl & ((1u << 12) | (1u << 13)))) return false;
-    *J = int(vid >> 1);
+    if ((vid >> 4) != PV_DENSES || __builtin_popcount(vid & 15u) != 1) return false;
+    *J = __builtin_ctz(vid & 15u);
     return true;
 }
 
@@ -333,7 +339,7 @@ static void emit_pass(const int (&r)[kPassBits], const std::vector<TileOp>& memb
         for (int j = 0; j < kPassBits; j++) {
             if (!byj[j]) continue;
             TileOp e = *byj[j];
-            if (head) e.pm.ctl = (kPvMulti + mask) | (uint32_t(__builtin_popcount(mask) - 1) << 8);
+            if (head) e.pm.ctl = (PV_DENSES << 4) | mask | (uint32_t(__builtin_popcount(mask) - 1) << 8);
             head = false;
             out.push_back(e);
         }

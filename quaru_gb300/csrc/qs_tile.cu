@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
                 if constexpr (REP == 3 && BLK)
                     if (kind == OP_BLOCK) block_apply(reinterpret_cast<float*>(s), tsize, op, bfrag);
             } else if (REP == 3 && kind == OP_PASS) {
-                if constexpr (REP == 3 && !BLK) pass_run_c64(reinterpret_cast<float2*>(s), tsize, base, &sops[o]);
+                if constexpr (REP == 3 && !BLK) pass_run_c64(reinterpret_cast<float2*>(s), tsize, &base, &sops[o]);
                 o += op.k;
             } else if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
                 const uint32_t tb = op.off[1];

@@ -29,13 +29,23 @@ constexpr uint8_t OP_PASS = 10;        // TileOp kind of a register-pass header
 // Codes of a k = 1 gate: dense complex 2x2, dense real 2x2, swap (the rows exchanged: X, CNOT),
 // swap with phases (Y), two-row phase (RZ); a k = 0 gate is a phase on one row (Z, S, phase, CZ).
 enum PassCode : uint32_t { PC_DENSE = 0, PC_REAL = 1, PC_SWAP = 2, PC_SWAPPH = 3, PC_DIAG2 = 4 };
-// Variant ids (PassMember::ctl bits 0-7): one dispatch per member, the kernel decodes nothing else.
-//   register gate, code c, register bit J, no register controls a:   c * 8 + J * 2 + a          0..39
-//   swap on register bit J controlled by register bit C (value 1):    40 + J * 4 + C             40..55
-//   dense gates on the register bits of mask M (2..4 gates, J order): 56 + M                    56..71
-//   lane gate, code c, no register controls a, no tuple controls n:   72 + c * 4 + a * 2 + n     72..91
-//   k = 0 phase, no register controls a:                              92 + a                     92..93
-constexpr uint32_t kPvSwapC = 40, kPvMulti = 56, kPvLane = 72, kPvPhase = 92;
+// Variant ids (PassMember::ctl bits 0-7): category in bits 4-7, its parameters in bits 0-3. The
+// kernel dispatches on them with a shallow tree of bit tests and decodes nothing else.
+//   0  dense gates with no controls on the register bits of mask M (1..4 gates, increasing bit
+//      order, coefficients in consecutive entries)                                  low = M
+//   1  swap on register bit J (X, CNOT with its control outside the registers)       low = J << 2 | all << 1
+//   2  swap on register bit J where register bit C is 1 (CNOT inside the registers)  low = J << 2 | C
+//   3  dense gate on a lane bit                                                      low = all << 1 | nocond
+//   4  swap on a lane bit                                                            low = all << 1 | nocond
+//   5  k = 0 phase                                                                   low = all << 1
+//   6, 7, 8, 9  register gate with controls: dense, real, swap with phases, two-row phase
+//                                                                                    low = J << 2 | all << 1
+//   10, 11, 12  lane gate: real, swap with phases, two-row phase                     low = all << 1 | nocond
+// all: no controls on the other register bits; nocond: no controls on tuple or lane bits.
+enum PassCat : uint32_t {
+    PV_DENSES = 0, PV_SWAP = 1, PV_SWAPC = 2, PV_LDENSE = 3, PV_LSWAP = 4, PV_PHASE = 5, PV_DENSE = 6,
+    PV_REAL = 7, PV_SWAPPH = 8, PV_DIAG2 = 9, PV_LREAL = 10, PV_LSWAPPH = 11, PV_LDIAG2 = 12
+};
 struct alignas(16) PassMember {
     float u[8];     // dense: row-major 2x2 complex; real: m00, m01, m10, m11; swap with phases and
                     // two-row phase: factor of row 0 (u[0..1]) and row 1 (u[2..3]); k = 0: u[0..1]

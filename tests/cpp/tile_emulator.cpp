@@ -100,17 +100,19 @@ void run_pass(std::vector<C>& s, uint32_t tsize, uint64_t tile_base, const std::
     for (int mi = 1; mi <= h.k;) {
         const qs::TileOp& m = tops[oi + mi];
         const qs::PassMember& g = m.pm;
-        const uint32_t vid = g.ctl & 255u;
-        const int adv = int((g.ctl >> 8) & 3u) + 1;
-        mi += adv;
+        const uint32_t vid = g.ctl & 255u, cat = vid >> 4, low = vid & 15u;
+        const int first = mi;
+        mi += int((g.ctl >> 8) & 3u) + 1;
         if ((g.ctl & (1u << 12)) && (tile_base & m.omask) != m.oval) continue;
         const bool cond = g.ctl & (1u << 13);
         int fm = g.fmv & 15, fv = (g.fmv >> 4) & 15;
-        if (vid >= qs::kPvLane && vid < qs::kPvPhase) {
-            const uint32_t c = vid - qs::kPvLane;
-            const int code = int(c / 4), t = int((g.ctl >> 10) & 3u);
-            if (c & 2) fm = fv = 0;
-            const bool nocond = c & 1;
+        const bool lane = cat == qs::PV_LDENSE || cat == qs::PV_LSWAP || cat >= qs::PV_LREAL;
+        if (lane) {
+            const int code = cat == qs::PV_LDENSE ? qs::PC_DENSE : cat == qs::PV_LSWAP ? qs::PC_SWAP
+                           : cat == qs::PV_LREAL ? qs::PC_REAL : cat == qs::PV_LSWAPPH ? qs::PC_SWAPPH : qs::PC_DIAG2;
+            const int t = int((g.ctl >> 10) & 3u);
+            if (low & 2u) fm = fv = 0;
+            const bool nocond = low & 1u;
             auto Y = X;
             for (uint32_t p = 0; p < ntup; p++) {
                 if (!nocond && (base[p] & g.om) != g.ov) continue;
@@ -118,10 +120,9 @@ void run_pass(std::vector<C>& s, uint32_t tsize, uint64_t tile_base, const std::
                 const int v = (base[p] >> t) & 1;
                 for (int j = 0; j < 16; j++) {
                     if ((j & fm) != fv) continue;
-                    const C x0 = v ? X[q][j] : X[p][j], x1 = v ? X[p][j] : X[q][j];
                     std::array<C, 16> pair{};
-                    pair[0] = x0;
-                    pair[1] = x1;
+                    pair[0] = v ? X[q][j] : X[p][j];
+                    pair[1] = v ? X[p][j] : X[q][j];
                     reg_gate(pair, code, 0, m.m, 0, 0);
                     Y[p][j] = pair[v];
                 }
@@ -130,23 +131,28 @@ void run_pass(std::vector<C>& s, uint32_t tsize, uint64_t tile_base, const std::
             continue;
         }
         for (uint32_t p = 0; p < ntup; p++) {
-            if (cond && (base[p] & g.om) != g.ov) continue;
             auto& x = X[p];
-            if (vid < qs::kPvSwapC) {
-                if (vid & 1u) fm = fv = 0;
-                reg_gate(x, int(vid / 8), int((vid % 8) / 2), m.m, fm, fv);
-            } else if (vid < qs::kPvMulti) {
-                const int J = int((vid - qs::kPvSwapC) / 4), Cb = int((vid - qs::kPvSwapC) % 4);
-                reg_gate(x, qs::PC_SWAP, J, m.m, 1 << Cb, 1 << Cb);
-            } else if (vid < qs::kPvLane) {
-                const uint32_t M = vid - qs::kPvMulti;
+            if (cat == qs::PV_DENSES) {  // no controls: every tuple
                 int e = 0;
                 for (int J = 0; J < 4; J++)
-                    if (M >> J & 1u) reg_gate(x, qs::PC_DENSE, J, tops[oi + (mi - adv) + e++].m, 0, 0);
-            } else {
-                if (vid & 1u) fm = fv = 0;
-                for (int j = 0; j < 16; j++)
-                    if ((j & fm) == fv) x[j] = cmul(m.m[0], m.m[1], x[j]);
+                    if (low >> J & 1u) reg_gate(x, qs::PC_DENSE, J, tops[oi + first + e++].m, 0, 0);
+                continue;
+            }
+            if (cond && (base[p] & g.om) != g.ov) continue;
+            const int J = int(low >> 2);
+            const int lfm = (low & 2u) ? 0 : fm, lfv = (low & 2u) ? 0 : fv;
+            switch (cat) {
+                case qs::PV_SWAP: reg_gate(x, qs::PC_SWAP, J, m.m, lfm, lfv); break;
+                case qs::PV_SWAPC: reg_gate(x, qs::PC_SWAP, J, m.m, 1 << (low & 3u), 1 << (low & 3u)); break;
+                case qs::PV_PHASE:
+                    for (int j = 0; j < 16; j++)
+                        if ((j & lfm) == lfv) x[j] = cmul(m.m[0], m.m[1], x[j]);
+                    break;
+                case qs::PV_DENSE: reg_gate(x, qs::PC_DENSE, J, m.m, lfm, lfv); break;
+                case qs::PV_REAL: reg_gate(x, qs::PC_REAL, J, m.m, lfm, lfv); break;
+                case qs::PV_SWAPPH: reg_gate(x, qs::PC_SWAPPH, J, m.m, lfm, lfv); break;
+                case qs::PV_DIAG2: reg_gate(x, qs::PC_DIAG2, J, m.m, lfm, lfv); break;
+                default: std::abort();
             }
         }
     }
