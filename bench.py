@@ -298,6 +298,7 @@ def run_ours(args) -> None:
             fused["blocks_tf32x3"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
                                       "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0)}
 
+    precision = None if args.no_precision else precision_section(q, torch, args)
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
     batch = None if args.no_batch else batch_section(q, args)
 
@@ -353,6 +354,7 @@ def run_ours(args) -> None:
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
         "clocks": clk,
         "fused": fused,
+        "precision_form": precision,
         "adjoint": adjoint,
         "batch": batch,
         "cpu_baseline": cpu,
@@ -361,6 +363,53 @@ def run_ours(args) -> None:
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def precision_section(q, torch, args) -> dict:
+    """The layered family at the bench's size for 40 layers: complex128 gate by gate (the plain FP64
+    form, the bench's arithmetic) against complex64 fused stages (register passes, and 5-qubit dense
+    blocks as 3xTF32 tensor-core GEMMs), with 1 - F = 1 - |<mixed|fp64>|^2 / (<mixed|mixed><fp64|fp64>)
+    accumulated in FP64 on the GPU after every 10 layers, and the gates/s of each form."""
+    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+
+    n = args.qubits
+    layers = layered_circuit(n, 40, seed_for(3))
+    torch.cuda.synchronize()
+    regs = {"fp64_plain": q.Register.from_int(n, 0),
+            "c64_passes": q.Register.from_int(n, 0, precision=q.QS_PREC_C64),
+            "c64_blocks_tf32x3": q.Register.from_int(n, 0, precision=q.QS_PREC_C64)}
+    regs["fp64_plain"].set_arith({"exact": q.QS_ARITH_EXACT, "fma": q.QS_ARITH_FMA,
+                                  "df64": q.QS_ARITH_DF64}[args.arith])
+    fuse = {"fp64_plain": 0, "c64_passes": 1, "c64_blocks_tf32x3": 2}
+    secs = {k: 0.0 for k in regs}
+    gates = 0
+    checkpoints = []
+    for k in range(4):
+        chunk = flatten(layers[10 * k:10 * k + 10])
+        gates += len(chunk)
+        for name, r in regs.items():
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            st = torch.cuda.ExternalStream(r.stream)
+            ev0.record(st)
+            r.apply_gates(chunk, fuse=fuse[name])
+            ev1.record(st)
+            ev1.synchronize()
+            secs[name] += ev0.elapsed_time(ev1) / 1e3
+        ref = regs["fp64_plain"]
+        nref = ref.inner_product(ref).real
+        cp = {"layers": 10 * (k + 1)}
+        for name in ("c64_passes", "c64_blocks_tf32x3"):
+            r = regs[name]
+            f = abs(r.inner_product(ref)) ** 2 / (nref * r.inner_product(r).real)
+            cp[f"one_minus_fidelity_{name}"] = 1.0 - f
+        checkpoints.append(cp)
+    out = {"workload": f"{n}-qubit layered family, 40 layers ({gates} gates), same seed as the main run",
+           "checkpoints": checkpoints,
+           "gates_per_s": {k: gates / v for k, v in secs.items()}}
+    out["mixed_vs_fp64_gates_per_s"] = {k: secs["fp64_plain"] / secs[k] for k in ("c64_passes", "c64_blocks_tf32x3")}
+    del regs
+    return out
 
 
 def adjoint_section(q, torch, args) -> dict:
@@ -501,6 +550,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused (tiled) circuit timing")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 40-layer precision-form section")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-gradient section")
     ap.add_argument("--kernels", action="store_true", help="run the per-kernel profiling workload instead")
     args = ap.parse_args()
