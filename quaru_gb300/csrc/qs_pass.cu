@@ -141,7 +141,7 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
         float2* s = bufs + size_t(b) * tsize;
         for (int o = 0; o < nops; o += int(sops[o].k) + 1) {
             if (o > 0) named_sync(1, NC);
-            pass_run_c64<NC>(s, tsize, &tbase[b], &sops[o]);
+            pass_run_c64<NC, true>(s, tsize, &tbase[b], &sops[o]);
         }
         fence_async_shared();  // this thread's writes, visible to the bulk stores
         mbar_arrive(&done[b]);

@@ -165,6 +165,9 @@ __device__ __forceinline__ void pv_phase(const float* u, int fm, int fv, float2 
 
 // Apply member m (its variant id in ctl) to the thread's registers. The dispatch is a shallow tree
 // of bit tests: a large switch costs about a hundred extra instructions per gate on sm_103a.
+// COMMON: only the variants pass_common() admits are compiled (fewer live registers; the stage
+// kernel with a copy warp runs at 96 registers per thread).
+template <bool COMMON>
 __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t base, float2 (&x)[16]) {
     const PassMember& g = m->pm;
     const uint32_t vid = ctl & 255u, cat = vid >> 4, low = vid & 15u;
@@ -190,7 +193,14 @@ __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t
             else pv_lane<C, false, false>(g, base, on, x);                    \
         }                                                                      \
     }
-        if (cat == PV_LDENSE) QS_PV_LANE(PC_DENSE) else QS_PV_LANE(PC_SWAP)
+        if (cat == PV_LDENSE) {
+            if (COMMON)
+                pv_lane<PC_DENSE, true, true>(g, base, on, x);
+            else
+                QS_PV_LANE(PC_DENSE)
+        } else {
+            QS_PV_LANE(PC_SWAP)
+        }
         return;
     }
     if (!on) return;  // register and phase gates: this tuple fails the controls
@@ -218,6 +228,7 @@ __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t
         if (all) pv_phase<true>(g.u, fm, fv, x); else pv_phase<false>(g.u, fm, fv, x);
         return;
     }
+    if (COMMON) return;
     // the rarer codes
     if (cat >= PV_LREAL) {
         if (cat == PV_LREAL) QS_PV_LANE(PC_REAL) else if (cat == PV_LSWAPPH) QS_PV_LANE(PC_SWAPPH) else QS_PV_LANE(PC_DIAG2)
@@ -250,7 +261,7 @@ __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t
 // with controls outside the tile). hdr is the OP_PASS header (its off[] and offsrc[] hold the 16
 // register offsets), its member entries follow it; threads 0..NT-1 take the 2^(T-4) tuples (a
 // multiple of 32) in turn.
-template <int NT = 256>
+template <int NT = 256, bool COMMON = false>
 __device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, const uint64_t* tile_base, const TileOp* hdr) {
     const int cnt = hdr->k;
     const uint32_t seg0 = hdr->seg[0], seg1 = hdr->seg[1], seg2 = hdr->seg[2], seg3 = hdr->seg[3],
@@ -269,7 +280,7 @@ __device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, const ui
         for (int mi = 1; mi <= cnt;) {
             const TileOp* m = hdr + mi;
             const uint32_t ctl = m->pm.ctl;
-            if (!(ctl & (1u << 12)) || (*tile_base & m->omask) == m->oval) pv_apply(m, ctl, base, x);
+            if (!(ctl & (1u << 12)) || (*tile_base & m->omask) == m->oval) pv_apply<COMMON>(m, ctl, base, x);
             mi += int((ctl >> 8) & 3u) + 1;
         }
 #pragma unroll

@@ -268,9 +268,12 @@ static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
         if (t.kind == OP_DENSE) {
             code = PC_DENSE;
             for (int i = 0; i < 8; i++) pm.u[i] = float(t.m[i]);
-        } else if (t.kind == OP_DENSE_REAL) {
+        } else if (t.kind == OP_DENSE_REAL && !(all && nocond && !t.omask)) {
             code = PC_REAL;
             for (int i = 0; i < 4; i++) pm.u[i] = float(t.m[2 * i]);
+        } else if (t.kind == OP_DENSE_REAL) {  // uncontrolled (H, RY): joins the dense groups
+            code = PC_DENSE;
+            for (int i = 0; i < 8; i++) pm.u[i] = float(t.m[i]);
         } else {
             // k = 1 monomial of a unitary: the rows exchanged (X, Y, CNOT) or kept (RZ), each with
             // a factor; the classifier drops untouched rows, so both rows are touched here.
@@ -434,8 +437,16 @@ std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStag
 
 bool pass_only(const std::vector<TileOp>& prog) {
     if (prog.empty()) return false;
-    for (size_t i = 0; i < prog.size(); i += size_t(prog[i].k) + 1)
+    for (size_t i = 0; i < prog.size(); i += size_t(prog[i].k) + 1) {
         if (prog[i].kind != OP_PASS) return false;
+        for (size_t j = i + 1; j <= i + prog[i].k;) {  // the member variants the copy-warp kernel compiles
+            const uint32_t ctl = prog[j].pm.ctl, cat = (ctl & 255u) >> 4, low = ctl & 15u;
+            const bool common = cat == PV_DENSES || cat == PV_SWAP || cat == PV_SWAPC || cat == PV_LSWAP ||
+                                cat == PV_PHASE || (cat == PV_LDENSE && low == 3u);
+            if (!common) return false;
+            j += ((ctl >> 8) & 3u) + 1;
+        }
+    }
     return true;
 }
 

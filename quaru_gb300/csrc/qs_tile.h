@@ -106,7 +106,9 @@ TileOp make_tile_op(const OpDesc& op, const TileStage& stage);
 // Pass scheduling moves a gate only past gates that share no qubit with it.
 std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStage& stage, bool passes);
 
-// Whether a stage program (from stage_program) consists of register passes only.
+// Whether a stage program (from stage_program) consists of register passes only, with the member
+// variants the copy-warp pass kernel compiles (uncontrolled dense groups, swaps, uncontrolled lane
+// dense gates, lane swaps, phases); other stages run in k_tile.
 bool pass_only(const std::vector<TileOp>& prog);
 
 // Launch the warp-specialised complex64 pass kernel for one pass-only stage whose program is

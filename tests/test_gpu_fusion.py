@@ -91,6 +91,29 @@ def test_fused_c64_within_tolerance():
     assert floored_rel_err(g.state, h.state) <= 1e-5
 
 
+@pytest.mark.parametrize("n,tile", [(12, 12), (15, 9), (15, 12), (18, 13), (20, 12)])
+def test_fused_c64_register_passes_full_gate_set(n, tile):
+    """complex64 stages over the whole gate mix (Haar, H, X, Y, Z, phase, CNOT, SWAP, Toffoli,
+    controlled-U, 0-controls, dense 2-qubit, a 6-qubit gate): register passes in the copy-warp kernel
+    (common variants; 4096- and 8192-amplitude tiles) and in the general tile kernel (the rest)."""
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+    from quaru_gb300 import operation as O
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    rng = np.random.default_rng(300 + n + tile)
+    ops = flatten(layered_circuit(n, 3, 900 + n)) + mixed_circuit(rng, n, 250)
+    ops += [O.hadamard(i) for i in range(n)] + [O.rz(0.1 * i + 0.05, i) for i in range(n)]
+    o = OracleRegister.from_int(n, 0)
+    o.apply_sequence([(g.matrix, g.targets) for g in ops])
+    g = q.Register.from_int(n, 0, precision=1)
+    g.apply_gates(ops, fuse=1, tile_qubits=tile)
+    assert floored_rel_err(g.state, o.state) <= 1e-4
+    h = q.Register.from_int(n, 0, precision=1)
+    h.apply_gates(ops, fuse=0)
+    assert floored_rel_err(g.state, h.state) <= 2e-5
+
+
 def test_fused_large_state_permutation_round_trip_bit_exact():
     """24 qubits: a permutation-and-phase circuit followed by its inverse restores the state exactly."""
     import quaru_gb300 as q
