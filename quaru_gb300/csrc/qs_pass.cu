@@ -1,9 +1,9 @@
 // qs_pass.cu — the warp-specialised stage kernel for complex64 stages made of register passes.
 //
-// A block is 8 compute warps and 1 copy warp. The copy warp keeps a ring of tile buffers in shared
-// memory filled with bulk copies (TMA) that complete on the buffer's `full` mbarrier, and writes a
-// finished tile back with bulk stores once the compute warps have arrived on its `done` mbarrier;
-// a buffer is refilled only after its stores have read it. The compute warps never issue or wait on
+// A block is 8 (or 16) compute warps and 1 copy warp. The copy warp keeps a ring of tile buffers in
+// shared memory filled with copies that complete on the buffer's `full` mbarrier (bulk TMA copies for
+// long rows, per-lane 16-byte cp.async for short ones), and writes a finished tile back once the
+// compute warps have arrived on its `done` mbarrier; a buffer is refilled only after it has been read. The compute warps never issue or wait on
 // copies themselves: per tile they wait for `full`, run the stage's register passes (a named
 // barrier among the 256 compute threads between passes), make their writes visible to the copy
 // engine and arrive on `done`. Every wait is bounded; one that gives up raises the error flag and
@@ -40,6 +40,7 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t tsize = 1u << pa.T;
     const int nbuf = pa.nbuf, nops = pa.op_end - pa.op_begin, nrows = 1 << pa.RH;
+    const bool bulk = nrows <= 8;
     // [tile buffers][full[4]][done[4]][tile base of each buffer[4]][ops (16-byte aligned)][row offsets]
     float2* bufs = reinterpret_cast<float2*>(smem_raw);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + size_t(nbuf) * (sizeof(float2) << pa.T));
@@ -62,7 +63,7 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
     }
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) {
-            mbar_init(&full[b], 1);
+            mbar_init(&full[b], bulk ? 1 : 33);  // bulk: lane 0's expect-tx; pieces: 32 lanes + lane 0's release
             mbar_init(&done[b], NC);
         }
         fence_mbar_init();
@@ -75,17 +76,34 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
 
     if (warp == NC / 32) {
         // ---------------------------------------------------------------- copy warp
+        // Long rows (>= 4 KiB): a few bulk copies per tile. Short rows: every bulk copy costs the
+        // copy engine ~90 cycles, so the lanes move the tile in 16-byte pieces instead (cp.async in,
+        // shared loads + global stores out), a warp instruction covering 512 contiguous bytes.
         const uint32_t row_bytes = uint32_t(sizeof(float2)) << pa.RL;
+        const uint32_t rmask = (1u << pa.RL) - 1u, chunks = tsize / 2;
         auto issue_load = [&](uint64_t i, int b) {
             const uint64_t tb = expand_index(first + i * gridDim.x, pa.outer);
-            if (lane == 0) {
-                tbase[b] = tb;  // released to the compute warps by the mbarrier's phase completion
-                mbar_expect_tx(&full[b], row_bytes * uint32_t(nrows));
+            float2* dst = bufs + size_t(b) * tsize;
+            if (bulk) {
+                if (lane == 0) {
+                    tbase[b] = tb;  // released to the compute warps by the mbarrier's phase completion
+                    mbar_expect_tx(&full[b], row_bytes * uint32_t(nrows));
+                }
+                __syncwarp();
+                for (int r = lane; r < nrows; r += 32)
+                    bulk_load(dst + (size_t(r) << pa.RL), state + tb + rowoff[r], row_bytes, &full[b]);
+            } else {
+#pragma unroll 8
+                for (uint32_t c = lane; c < chunks; c += 32) {
+                    const uint32_t a = 2 * c;
+                    cp_async16(dst + a, state + tb + rowoff[a >> pa.RL] + (a & rmask));
+                }
+                cp_async_mbar_arrive(&full[b]);  // one arrival per lane once its copies have landed
+                if (lane == 0) {
+                    tbase[b] = tb;
+                    mbar_arrive(&full[b]);  // releases tbase[b]
+                }
             }
-            __syncwarp();
-            for (int r = lane; r < nrows; r += 32)
-                bulk_load(bufs + size_t(b) * tsize + (size_t(r) << pa.RL), state + tb + rowoff[r], row_bytes,
-                          &full[b]);
         };
         uint64_t issued = 0;
         for (; issued < nmy && issued < uint64_t(nbuf); issued++) issue_load(issued, int(issued));
@@ -103,18 +121,30 @@ __global__ void __maxnreg__(96) k_pass(float2* __restrict__ state, uint64_t ntil
             }
             dphase ^= 1u << b;
             const uint64_t base = expand_index(first + j * gridDim.x, pa.outer);
-            for (int r = lane; r < nrows; r += 32)
-                bulk_store(state + base + rowoff[r], bufs + size_t(b) * tsize + (size_t(r) << pa.RL), row_bytes);
-            bulk_commit();
-            if (issued < nmy) {  // tile `issued` = j + nbuf takes this buffer once the stores have read it
-                bulk_wait_read<0>();
+            float2* src = bufs + size_t(b) * tsize;
+            if (bulk) {
+                for (int r = lane; r < nrows; r += 32)
+                    bulk_store(state + base + rowoff[r], src + (size_t(r) << pa.RL), row_bytes);
+                bulk_commit();
+            } else {
+                // each lane stores exactly the pieces it loads, so its own later cp.async into this
+                // buffer cannot overtake these shared-memory reads
+#pragma unroll 8
+                for (uint32_t c = lane; c < chunks; c += 32) {
+                    const uint32_t a = 2 * c;
+                    const float4 v = *reinterpret_cast<const float4*>(src + a);
+                    *reinterpret_cast<float4*>(state + base + rowoff[a >> pa.RL] + (a & rmask)) = v;
+                }
+            }
+            if (issued < nmy) {  // tile `issued` = j + nbuf takes this buffer once it has been read
+                if (bulk) bulk_wait_read<0>();
                 __syncwarp();
                 issue_load(issued, b);
                 issued++;
             }
             b = (b + 1 == nbuf) ? 0 : b + 1;
         }
-        bulk_wait_all();
+        if (bulk) bulk_wait_all();
         if (!ok) {
             if (lane == 0) {
                 s_abort = 1;
