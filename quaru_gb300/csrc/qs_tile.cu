@@ -393,8 +393,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
             if (r >> b & 1) o |= 1ull << sa.rhigh[b];
         rowoff[r] = o;
     }
+    // Long rows (at most 8 per tile): warp 0 moves the tile with bulk copies. Short
+    // rows: each bulk copy costs the copy engine ~90 cycles, so all threads move the tile in 16-byte
+    // pieces (cp.async in, shared loads + global stores out), two tiles ahead in a ring of three.
+    const bool bulk = nrows <= 8;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < nbuf; b++) mbar_init(&mbar[b], 1);
+        for (int b = 0; b < nbuf; b++) mbar_init(&mbar[b], bulk ? 1 : kTileThreads);
         fence_mbar_init();
         s_abort = 0;
     }
@@ -404,29 +408,53 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
     const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.RL;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     GE* gstate = static_cast<GE*>(state);
-    auto issue_load = [&](uint64_t i, int b) {  // warp 0 only
+    constexpr uint32_t kPer = 16 / sizeof(GE);  // amplitudes per 16-byte piece
+    const uint32_t rmask = (1u << sa.RL) - 1u, pieces = tsize / kPer;
+    auto issue_load = [&](uint64_t i, int b) {  // bulk: warp 0 only; pieces: every thread
         const uint64_t tb = expand_index(first + i * gridDim.x, sa.outer);
-        if (lane == 0) mbar_expect_tx(&mbar[b], row_bytes * uint32_t(nrows));
-        __syncwarp();
-        for (int r = lane; r < nrows; r += 32)
-            bulk_load(bufs + size_t(b) * tsize + (size_t(r) << sa.RL), gstate + tb + rowoff[r], row_bytes, &mbar[b]);
+        GE* dst = reinterpret_cast<GE*>(bufs + size_t(b) * tsize);
+        if (bulk) {
+            if (lane == 0) mbar_expect_tx(&mbar[b], row_bytes * uint32_t(nrows));
+            __syncwarp();
+            for (int r = lane; r < nrows; r += 32)
+                bulk_load(dst + (size_t(r) << sa.RL), gstate + tb + rowoff[r], row_bytes, &mbar[b]);
+        } else {
+            for (uint32_t c = threadIdx.x; c < pieces; c += kTileThreads) {
+                const uint32_t a = c * kPer;
+                cp_async16(dst + a, gstate + tb + rowoff[a >> sa.RL] + (a & rmask));
+            }
+            cp_async_mbar_arrive(&mbar[b]);
+        }
     };
-    if (warp == 0 && nmy > 0) issue_load(0, 0);
+    const int ahead = bulk ? 1 : nbuf - 1;  // tiles in flight beyond the one being computed
+    if (bulk) {
+        if (warp == 0 && nmy > 0) issue_load(0, 0);
+    } else {
+        for (int k = 0; k < ahead && uint64_t(k) < nmy; k++) issue_load(uint64_t(k), k);
+    }
     uint64_t it = 0;
     int bsel = 0;          // buffer of tile it
     uint32_t phase = 0;    // bit b: parity of buffer b's next completion
     for (; it < nmy; it++) {
         E* s = bufs + size_t(bsel) * tsize;
         const uint64_t base = expand_index(first + it * gridDim.x, sa.outer);
-        if (warp == 0 && it + 1 < nmy) {
-            // Tile it + 1 reuses the buffer of tile it + 1 - nbuf, whose stores were committed
-            // nbuf - 1 groups ago: wait until those have read shared memory.
-            if (nbuf == 3)
-                bulk_wait_read<1>();
-            else
-                bulk_wait_read<0>();
-            __syncwarp();
-            issue_load(it + 1, bsel + 1 == nbuf ? 0 : bsel + 1);
+        if (bulk) {
+            if (warp == 0 && it + 1 < nmy) {
+                // Tile it + 1 reuses the buffer of tile it + 1 - nbuf, whose stores were committed
+                // nbuf - 1 groups ago: wait until those have read shared memory.
+                if (nbuf == 3)
+                    bulk_wait_read<1>();
+                else
+                    bulk_wait_read<0>();
+                __syncwarp();
+                issue_load(it + 1, bsel + 1 == nbuf ? 0 : bsel + 1);
+            }
+        } else if (it + ahead < nmy) {
+            // tile it + ahead takes the buffer of tile it + ahead - nbuf = it - 1, written back at
+            // the end of the previous iteration by the same threads that now load into it
+            int nb = bsel + ahead;
+            if (nb >= nbuf) nb -= nbuf;
+            issue_load(it + ahead, nb);
         }
         if (!mbar_wait_bounded(&mbar[bsel], (phase >> bsel) & 1u)) atomicOr(&s_abort, 1);
         phase ^= 1u << bsel;
@@ -494,21 +522,36 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
                     make_double2(__dadd_rn(df_f2d(f.x), df_f2d(f.y)), __dadd_rn(df_f2d(f.z), df_f2d(f.w)));
             }
         }
-        fence_async_shared();  // make this tile's shared-memory writes visible to the bulk stores
-        __syncthreads();
-        if (warp == 0) {
-            for (int r = lane; r < nrows; r += 32)
-                bulk_store(gstate + base + rowoff[r], s + (size_t(r) << sa.RL), row_bytes);
-            bulk_commit();
+        if (bulk) {
+            fence_async_shared();  // make this tile's shared-memory writes visible to the bulk stores
+            __syncthreads();
+            if (warp == 0) {
+                for (int r = lane; r < nrows; r += 32)
+                    bulk_store(gstate + base + rowoff[r], s + (size_t(r) << sa.RL), row_bytes);
+                bulk_commit();
+            }
+        } else {
+            __syncthreads();
+            const GE* src = reinterpret_cast<const GE*>(s);
+            for (uint32_t c = threadIdx.x; c < pieces; c += kTileThreads) {
+                const uint32_t a = c * kPer;
+                *reinterpret_cast<float4*>(gstate + base + rowoff[a >> sa.RL] + (a & rmask)) =
+                    *reinterpret_cast<const float4*>(src + a);
+            }
         }
         bsel = bsel + 1 == nbuf ? 0 : bsel + 1;
     }
-    if (warp == 0) bulk_wait_all();
-    if (s_abort && threadIdx.x == 0) {
-        atomicExch(err, 1);
-        // the load of tile it + 1 may still be in flight: wait for it (bounded) before exiting
-        const int nb = bsel + 1 == nbuf ? 0 : bsel + 1;
-        if (it + 1 < nmy) mbar_wait_bounded(&mbar[nb], (phase >> nb) & 1u);
+    if (bulk) {
+        if (warp == 0) bulk_wait_all();
+        if (s_abort && threadIdx.x == 0) {
+            atomicExch(err, 1);
+            // the load of tile it + 1 may still be in flight: wait for it (bounded) before exiting
+            const int nb = bsel + 1 == nbuf ? 0 : bsel + 1;
+            if (it + 1 < nmy) mbar_wait_bounded(&mbar[nb], (phase >> nb) & 1u);
+        }
+    } else {
+        cp_async_wait_all();  // copies of tiles the loop did not reach
+        if (s_abort && threadIdx.x == 0) atomicExch(err, 1);
     }
 }
 
