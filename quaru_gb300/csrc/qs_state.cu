@@ -31,6 +31,11 @@ static int grid_cap(uint64_t work, int sms, int per_thread = 1) {
 
 __device__ __forceinline__ double2 to_d2(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(double(v.x), double(v.y)); }
+// Reductions and the collapse read complex64 amplitudes through an integer-pipe conversion: the FP64
+// pipe (~1/64 of the FP32 rate on GB300) is left to the sums and quotients themselves. Exact for
+// normal floats; subnormal floats (< 2^-126) read as zero, far below every tolerance they feed.
+__device__ __forceinline__ double2 to_d2_int(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d2_int(float2 v) { return make_double2(df_f2d(v.x), df_f2d(v.y)); }
 __device__ __forceinline__ void from_d2(double2* dst, double2 v) { *dst = v; }
 __device__ __forceinline__ void from_d2(float2* dst, double2 v) { *dst = make_float2(float(v.x), float(v.y)); }
 
@@ -126,8 +131,8 @@ __global__ void __launch_bounds__(kT) k_prob_partials(const T* __restrict__ st, 
     double p0 = 0.0, p1 = 0.0;
     for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
         const uint64_t i0 = ((t & ~lo_mask) << 1) | (t & lo_mask);
-        const double2 a = to_d2(st[i0]);
-        const double2 b = to_d2(st[i0 | tb]);
+        const double2 a = to_d2_int(st[i0]);
+        const double2 b = to_d2_int(st[i0 | tb]);
         p0 = fma(a.x, a.x, p0);
         p0 = fma(a.y, a.y, p0);
         p1 = fma(b.x, b.x, p1);
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t np
     for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
         const uint64_t i0 = ((t & ~lo_mask) << 1) | (t & lo_mask);
         const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
-        const double2 x = to_d2(st[keep]);
+        const double2 x = to_d2_int(st[keep]);
         double2 y;
         if (TRUEDIV) {
             y.x = x.x / d;
