@@ -498,8 +498,10 @@ def _measure_probs(lib, reg, target: int) -> float:
 
 def run_kernels(args) -> None:
     """A small workload that launches every kernel family once per repetition (for ncu captures):
-    init, dense 1-qubit (exact, FMA, DF64), CNOT/permutation, dense 3-qubit, probability reduction
-    and collapse, tiles (complex128 DF64, complex64 groups, complex64 3xTF32 blocks), adjoint, batch."""
+    init (basis and product state), dense 1-qubit (exact, FMA, DF64; complex64), CNOT/permutation,
+    dense 3-qubit, 6-qubit permutation and dense gates, probability reduction, read-back and
+    collapse (both precisions), stages (complex128 DF64 tiles, complex64 register passes, complex64
+    3xTF32 blocks), adjoint, batch."""
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
@@ -521,10 +523,20 @@ def run_kernels(args) -> None:
         r.try_apply_fast(O.Operation(u3, [0, n // 2, n - 3]))
         r.measure(n - 1, 0.5)
         r.apply_gates(layers, fuse=1)
+        # wide gates (out-of-place kernels), a product-state register, the probability read-back
+        perm = np.eye(64)[np.random.default_rng(2).permutation(64)]
+        r.try_apply_fast(O.Operation(perm, [0, 3, 7, 11, n - 5, n - 2]))
+        r.try_apply_fast(O.Operation(np.linalg.qr(rng.normal(size=(64, 64)) + 1j * rng.normal(size=(64, 64)))[0],
+                                     [1, 4, 6, 9, n - 4, n - 1]))
+        pq = [np.array([[np.cos(0.1 * i)], [np.sin(0.1 * i)]], dtype=complex) for i in range(n)]
+        p_reg = q.Register.try_from_qubits(pq)
+        p_reg.probabilities()
         c = q.Register.from_int(n, 0, precision=q.QS_PREC_C64)
+        c.apply_gates(layers[:len(layers) // 2], fuse=0)
         c.apply_gates(layers, fuse=1)
         c.apply_gates(layers, fuse=2)
-        del r, c
+        c.measure(n - 1, 0.5)
+        del r, c, p_reg
     gates, params, terms = config4()
     reg = q.Register.from_int(20, 0)
     reg.set_arith(q.QS_ARITH_FMA)

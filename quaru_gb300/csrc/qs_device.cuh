@@ -141,6 +141,21 @@ __device__ __forceinline__ double df_f2d(float f) {
     return (mag >= 0x00800000u) ? __hiloint2double(int(hi), int(b << 29)) : 0.0;
 }
 
+// double -> float rounded to nearest even with integer operations, for values whose float lies in
+// the normal range (|v| >= 2^-126 and finite; smaller values give zero, larger ones infinity).
+__device__ __forceinline__ float d2f_int(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const uint32_t sign = uint32_t(b >> 32) & 0x80000000u;
+    const int e = int((b >> 52) & 0x7ffu) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    uint32_t r = (uint32_t(e) << 23) | uint32_t(m >> 29);
+    const uint32_t rest = uint32_t(m & 0x1fffffffull);  // the 29 dropped bits
+    if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) r += 1u;  // a carry may bump the exponent
+    return __uint_as_float(sign | r);
+}
+
 __device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
     s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);

@@ -6,6 +6,7 @@
 // combination), the outcome decision on the host, then one collapse sweep.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -80,18 +81,43 @@ cudaError_t launch_init_basis(void* state, int n, int prec, uint64_t index, cuda
     return counted(cudaGetLastError());
 }
 
+// One doubling level of the same fold: the partial product after qubits 0..j-1 depends only on the
+// low j bits of the index, so st[0, half) holding those partials becomes
+// st[b * half + k] = q_j[b] * st[k] for b = 0, 1: the very products the per-amplitude loop forms at
+// step j, computed once per partial instead of once per amplitude.
+__global__ void __launch_bounds__(kT) k_product_level(double2* __restrict__ st, uint64_t half, double q0r, double q0i,
+                                                      double q1r, double q1i) {
+    const uint64_t stride = uint64_t(gridDim.x) * kT;
+    for (uint64_t k = uint64_t(blockIdx.x) * kT + threadIdx.x; k < half; k += stride) {
+        const double2 v = st[k];
+        st[k + half] = cmul_exact(q1r, q1i, v);
+        st[k] = cmul_exact(q0r, q0i, v);
+    }
+}
+
 cudaError_t launch_init_product(void* state, int n, int prec, const double* qubits, cudaStream_t s, int sms) {
     ProductArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.n = n;
-    for (int j = 0; j < n; j++)
+    // complex128: the first 16 qubits per amplitude, the rest by doubling levels (2^(n+1) products
+    // in all instead of n * 2^n). complex64 keeps the whole product in double and rounds it once.
+    const int n0 = (prec == QS_PREC_C64) ? n : std::min(n, 16);
+    a.n = n0;
+    for (int j = 0; j < n0; j++)
         for (int c = 0; c < 4; c++) a.q[j][c] = qubits[4 * j + c];
-    const uint64_t N = 1ull << n;
-    if (prec == QS_PREC_C64)
-        k_init_product<float2><<<grid_cap(N, sms), kT, 0, s>>>((float2*)state, N, a);
-    else
-        k_init_product<double2><<<grid_cap(N, sms), kT, 0, s>>>((double2*)state, N, a);
-    return counted(cudaGetLastError());
+    const uint64_t N0 = 1ull << n0;
+    if (prec == QS_PREC_C64) {
+        k_init_product<float2><<<grid_cap(N0, sms), kT, 0, s>>>((float2*)state, N0, a);
+        return counted(cudaGetLastError());
+    }
+    k_init_product<double2><<<grid_cap(N0, sms), kT, 0, s>>>((double2*)state, N0, a);
+    cudaError_t e = counted(cudaGetLastError());
+    for (int j = n0; j < n && e == cudaSuccess; j++) {
+        const uint64_t half = 1ull << j;
+        const double* q = qubits + 4 * j;
+        k_product_level<<<grid_cap(half, sms), kT, 0, s>>>((double2*)state, half, q[0], q[1], q[2], q[3]);
+        e = counted(cudaGetLastError());
+    }
+    return e;
 }
 
 // ---------------------------------------------------------------- measurement
@@ -190,6 +216,15 @@ __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t np
     for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
         const uint64_t i0 = ((t & ~lo_mask) << 1) | (t & lo_mask);
         const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
+        if constexpr (sizeof(T) == 8 && !TRUEDIV) {
+            // complex64: one FP64 multiply by RN(1/d) per component, rounded to float on the
+            // integer pipe (the quotient is stored as a float, so the exactly rounded double
+            // quotient of the complex128 path buys nothing here)
+            const double2 x = to_d2_int(st[keep]);
+            st[keep] = T{d2f_int(x.x * rinv), d2f_int(x.y * rinv)};
+            st[drop] = T{0.0f, 0.0f};
+            continue;
+        }
         const double2 x = to_d2_int(st[keep]);
         double2 y;
         if (TRUEDIV) {

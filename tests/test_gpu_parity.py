@@ -197,6 +197,26 @@ def test_measure_matches_oracle(q, orc):
             assert floored_rel_err(g.state, o.state) <= 1e-13
 
 
+def test_c64_collapse_rounding(q):
+    """complex64 collapse: x * RN(1/sqrt(total)) in FP64, rounded to float (nearest even) on the
+    integer pipe: bit-identical to numpy's float64 product cast to float32."""
+    rng = np.random.default_rng(702)
+    n = 12
+    st = (rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)).astype(np.complex64)
+    st /= np.float32(np.linalg.norm(st.astype(np.complex128)))
+    g = q.Register.from_int(n, 0, precision=1)
+    g.state = st
+    target = 3
+    out = g.measure(target, 0.4)
+    p0, p1 = g.last_probs
+    rinv = 1.0 / math.sqrt(p1 if out else p0)
+    exp = np.zeros_like(st)
+    keep = ((np.arange(1 << n) >> target) & 1) == int(out)
+    exp.real[keep] = (st.real[keep].astype(np.float64) * rinv).astype(np.float32)
+    exp.imag[keep] = (st.imag[keep].astype(np.float64) * rinv).astype(np.float32)
+    assert np.array_equal(g.state, exp.astype(np.complex128))  # float values read back exactly
+
+
 def test_measure_outcome_rule_and_collapse_exact(q, orc):
     # draw == prob_0 exactly gives false (x > prob_0 is false), src/register.rs:321
     g = q.Register.new([False, False]).apply(__import__("quaru_gb300").operation.hadamard(0))
@@ -239,9 +259,10 @@ def test_state_roundtrip_probabilities_clone_eq(q, orc):
     assert g.size() == n and g64.precision == 1
 
 
-def test_from_qubits_product_state_bit_exact(q, orc):
-    rng = np.random.default_rng(900)
-    n = 10
+@pytest.mark.parametrize("n", [10, 20])
+def test_from_qubits_product_state_bit_exact(q, orc, n):
+    """n = 20 also covers the doubling levels above the first 16 qubits."""
+    rng = np.random.default_rng(900 + n)
     qs = []
     for _ in range(n):
         v = rng.normal(size=2) + 1j * rng.normal(size=2)
