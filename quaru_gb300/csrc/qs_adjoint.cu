@@ -19,7 +19,9 @@
 #include "qs_circuit.h"
 #include "qs_device.cuh"
 #include "qs_kernels.h"
+#include "qs_pass.cuh"
 #include "qs_reduce.cuh"
+#include "qs_tile.h"
 
 namespace qs {
 
@@ -193,6 +195,169 @@ __global__ void __launch_bounds__(kAT) k_grad_final(const double* __restrict__ p
     if (threadIdx.x == 0) out[blockIdx.x] = a;
 }
 
+// ---------------------------------------------------------------- tiled reverse sweep
+// One stage of the reverse sweep over tiles of 2^T amplitudes: psi and lambda tiles side by side in
+// shared memory, the stage's gates taken in reverse order. A rotation adds Im<lambda|A|psi> over the
+// tile's pairs to its slot (FP64, per warp, in shared memory) and is un-applied from both tiles; a
+// fixed gate (its inverse) is applied to both. Gates were reordered only past gates on disjoint
+// qubits, with which they commute, so every inner product equals the one of the gate-by-gate sweep.
+constexpr int kAdjT = 11;           // tile qubits of the reverse sweep
+constexpr int kAdjThreads = 256;
+constexpr int kAdjMaxRot = 64;      // rotations per stage
+
+struct AdjOpDev {
+    TileOp t;      // tile-local form (target bit, tuple expansion, controls, matrix of a fixed gate)
+    int rot;       // stage-local rotation slot, or -1 for a fixed gate
+    int axis;      // QS_GATE_RX / RY / RZ
+    double c, s;   // cos(theta/2), -sin(theta/2): the inverse rotation
+    int pad_[2];
+};
+
+struct AdjStageArgs {
+    int T, RL, RH;
+    int nops, nrot;
+    IndexMap outer;
+    uint8_t rhigh[kTileMaxHigh];
+    int slot[kAdjMaxRot];  // global rotation slot of each stage-local slot
+};
+
+template <typename T>
+__device__ __forceinline__ void adj_fixed(T* s, const TileOp& op, uint32_t tsize) {
+    using R = decltype(T().x);
+    const uint32_t ntup = tsize >> op.npos;
+    uint32_t seg[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) seg[j] = op.seg[j];
+    if (op.kind == OP_DENSE || op.kind == OP_DENSE_REAL) {
+        const uint32_t tb = op.off[1];
+        const R m0 = R(op.m[0]), m1 = R(op.m[1]), m2 = R(op.m[2]), m3 = R(op.m[3]);
+        const R m4 = R(op.m[4]), m5 = R(op.m[5]), m6 = R(op.m[6]), m7 = R(op.m[7]);
+        for (uint32_t p = threadIdx.x; p < ntup; p += kAdjThreads) {
+            const uint32_t i0 = tuple_index(p, op.npos, seg, op.pos, op.lfixval);
+            const T a = s[i0], b = s[i0 | tb];
+            T y0 = cfma(m2, m3, b, czero<T>());
+            y0 = cfma(m0, m1, a, y0);
+            T y1 = cfma(m6, m7, b, czero<T>());
+            y1 = cfma(m4, m5, a, y1);
+            s[i0] = y0;
+            s[i0 | tb] = y1;
+        }
+        return;
+    }
+    const int D = 1 << op.k;  // monomial: permutation with factors
+    for (uint32_t p = threadIdx.x; p < ntup; p += kAdjThreads) {
+        const uint32_t i0 = tuple_index(p, op.npos, seg, op.pos, op.lfixval);
+        T y[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+            if (r < D && op.pf[r] != PF_SKIP_DEV) y[r] = s[i0 + op.offsrc[r]];
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            if (r >= D || op.pf[r] == PF_SKIP_DEV) continue;
+            T v = y[r];
+            if (op.pf[r] == 255) {
+                const R pr = R(op.m[2 * r]), pi = R(op.m[2 * r + 1]);
+                v = cfma(pr, pi, y[r], czero<T>());
+            } else {
+                v = apply_pf(y[r], op.pf[r]);
+            }
+            s[i0 + op.off[r]] = v;
+        }
+    }
+}
+
+template <typename T, int AXIS>
+__device__ __forceinline__ double adj_rot_tile(T* sp, T* sl, const AdjOpDev& op, uint32_t tsize) {
+    using R = decltype(T().x);
+    const TileOp& t = op.t;
+    uint32_t seg[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) seg[j] = t.seg[j];
+    const uint32_t tb = 1u << t.tb[0];
+    const R c = R(op.c), sn = R(op.s);
+    double acc = 0.0;
+    DfAcc facc;
+    for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += kAdjThreads) {
+        const uint32_t i0 = tuple_index(p, t.npos, seg, t.pos, 0u), i1 = i0 | tb;
+        T a = sp[i0], b = sp[i1], l0 = sl[i0], l1 = sl[i1];
+        if constexpr (sizeof(R) == 8)
+            acc += im_term<AXIS>(l0, l1, a, b);
+        else
+            im_term_acc<AXIS>(facc, l0, l1, a, b);
+        rot_pair<AXIS>(c, sn, a.x, a.y, b.x, b.y);
+        rot_pair<AXIS>(c, sn, l0.x, l0.y, l1.x, l1.y);
+        sp[i0] = a;
+        sp[i1] = b;
+        sl[i0] = l0;
+        sl[i1] = l1;
+    }
+    if constexpr (sizeof(R) == 4) acc = __dadd_rn(df_f2d(facc.s), df_f2d(facc.c));
+    return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, T* __restrict__ lam, uint64_t ntiles,
+                                                           const __grid_constant__ AdjStageArgs a,
+                                                           const AdjOpDev* __restrict__ ops,
+                                                           double* __restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t tsize = 1u << a.T;
+    T* sp = reinterpret_cast<T*>(smem_raw);
+    T* sl = sp + tsize;
+    double* sacc = reinterpret_cast<double*>(sl + tsize);  // [nrot][8 warps]
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sacc + size_t(a.nrot) * (kAdjThreads / 32));
+    const int nrows = 1 << a.RH, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < a.nrot * (kAdjThreads / 32); i += kAdjThreads) sacc[i] = 0.0;
+    for (int r = threadIdx.x; r < nrows; r += kAdjThreads) {
+        uint64_t o = 0;
+        for (int b = 0; b < a.RH; b++)
+            if (r >> b & 1) o |= 1ull << a.rhigh[b];
+        rowoff[r] = o;
+    }
+    __syncthreads();
+    const uint32_t rmask = (1u << a.RL) - 1u;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t base = expand_index(tile, a.outer);
+        for (uint32_t i = threadIdx.x; i < tsize; i += kAdjThreads) {
+            const uint64_t g = base + rowoff[i >> a.RL] + (i & rmask);
+            sp[i] = psi[g];
+            sl[i] = lam[g];
+        }
+        __syncthreads();
+        for (int o = 0; o < a.nops; o++) {
+            const AdjOpDev& op = ops[o];
+            if ((base & op.t.omask) != op.t.oval) continue;  // the same for the whole block
+            if (op.rot >= 0) {
+                double v;
+                if (op.axis == QS_GATE_RX)
+                    v = adj_rot_tile<T, QS_GATE_RX>(sp, sl, op, tsize);
+                else if (op.axis == QS_GATE_RY)
+                    v = adj_rot_tile<T, QS_GATE_RY>(sp, sl, op, tsize);
+                else
+                    v = adj_rot_tile<T, QS_GATE_RZ>(sp, sl, op, tsize);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+                if (lane == 0) sacc[op.rot * (kAdjThreads / 32) + warp] += v;
+            } else {
+                adj_fixed(sp, op.t, tsize);
+                adj_fixed(sl, op.t, tsize);
+            }
+            __syncthreads();
+        }
+        for (uint32_t i = threadIdx.x; i < tsize; i += kAdjThreads) {
+            const uint64_t g = base + rowoff[i >> a.RL] + (i & rmask);
+            psi[g] = sp[i];
+            lam[g] = sl[i];
+        }
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < a.nrot; r += kAdjThreads) {
+        double v = 0.0;
+        for (int w = 0; w < kAdjThreads / 32; w++) v += sacc[r * (kAdjThreads / 32) + w];
+        partials[size_t(a.slot[r]) * gridDim.x + blockIdx.x] = v;
+    }
+}
+
 // ---------------------------------------------------------------- host side
 static int fail(cudaError_t e, const char* what, std::string* msg) {
     if (msg) *msg = std::string(what) + ": " + cudaGetErrorString(e);
@@ -296,6 +461,132 @@ static void launch_adj_rot(int kind, void* psi, void* lam, int n, int q, const d
     note_launches(1);
 }
 
+// R_A(theta) as a row-major interleaved 2x2 matrix (the convention of rot_pair).
+static std::vector<double> rotation_matrix(int axis, double c, double s) {
+    if (axis == QS_GATE_RX) return {c, 0, 0, -s, 0, -s, c, 0};
+    if (axis == QS_GATE_RY) return {c, 0, -s, 0, s, 0, c, 0};
+    return {c, -s, 0, 0, 0, 0, c, s};
+}
+
+// Grid of the tiled reverse sweep for n qubits (the same for every stage, so partials line up).
+template <typename T>
+static int adj_grid(int n, int sms) {
+    const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 + (8u << 6);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_adj_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<T>, kAdjThreads, smem);
+    const uint64_t ntiles = 1ull << (n - kAdjT);
+    return int(std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm))));
+}
+
+// The reverse sweep as tiled stages: gates m-1 .. 0, rotations with their inner products, fixed
+// gates as their inverses (inv). Partials of rotation slot r land in part[r * grid .. + grid).
+template <typename T>
+static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, const qs_param_gate* gates, size_t m,
+                         const double* params, const std::vector<int>& rot_slot, const std::vector<OpDesc>& inv,
+                         double* part, int grid, cudaStream_t s, int sms, std::string* msg) {
+    std::vector<OpDesc> rops;
+    std::vector<int> src;
+    for (size_t gg = m; gg-- > 0;) {
+        if (rot_slot[gg] >= 0) {  // planning form: a dense 1-qubit gate on the rotation's target
+            OpDesc d;
+            d.kind = OP_DENSE;
+            d.k = d.orig_k = 1;
+            d.tq[0] = int(gates[gg].targets[0]);
+            d.m.assign(8, 0.0);
+            d.touched_rows = 2;
+            rops.push_back(std::move(d));
+        } else {
+            rops.push_back(inv[gg]);
+        }
+        src.push_back(int(gg));
+    }
+    const std::vector<TileStage> stages = plan_tiles(rops, n, kAdjT, 5, false);
+    // device tables: every stage's ops (split so a launch holds at most kAdjMaxRot rotations)
+    std::vector<AdjOpDev> host;
+    struct Launch {
+        int stage, first, count, nrot;
+        int slot[kAdjMaxRot];
+    };
+    std::vector<Launch> launches;
+    for (size_t si = 0; si < stages.size(); si++) {
+        const TileStage& st = stages[si];
+        if (!st.tiled) {
+            launches.push_back(Launch{int(si), -1, 0, 0, {}});
+            continue;
+        }
+        Launch cur{int(si), int(host.size()), 0, 0, {}};
+        for (int idx : st.ops) {
+            const int g = src[idx];
+            if (rot_slot[g] >= 0 && cur.nrot == kAdjMaxRot) {
+                launches.push_back(cur);
+                cur = Launch{int(si), int(host.size()), 0, 0, {}};
+            }
+            AdjOpDev e;
+            std::memset(&e, 0, sizeof(e));
+            e.t = make_tile_op(rops[idx], st);
+            e.rot = -1;
+            if (rot_slot[g] >= 0) {
+                const double th = params[gates[g].param];
+                e.rot = cur.nrot;
+                cur.slot[cur.nrot++] = rot_slot[g];
+                e.axis = gates[g].kind;
+                e.c = std::cos(0.5 * th);
+                e.s = -std::sin(0.5 * th);
+            }
+            host.push_back(e);
+            cur.count++;
+        }
+        launches.push_back(cur);
+    }
+    AdjOpDev* dops = nullptr;
+    if (!host.empty()) {
+        cudaError_t e = cudaMallocAsync((void**)&dops, host.size() * sizeof(AdjOpDev), s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(AdjOpDev), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return fail(e, "reverse-sweep tables", msg);
+    }
+    int rc = QS_OK;
+    const uint64_t ntiles = 1ull << (n - kAdjT);
+    for (const Launch& L : launches) {
+        const TileStage& st = stages[L.stage];
+        if (L.first < 0) {  // a gate no tile holds: its inverse on psi and lambda, one sweep each
+            const OpDesc& op = rops[st.single];
+            if ((rc = apply_op(state, n, prec, arith, op, s, sms, msg)) != QS_OK) break;
+            if ((rc = apply_op(lam, n, prec, arith, op, s, sms, msg)) != QS_OK) break;
+            continue;
+        }
+        AdjStageArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.T = st.T;
+        const int H = int(st.high.size());
+        int run = 0;
+        while (run < H && st.high[run] == st.L + run) run++;
+        a.RL = st.L + run;
+        a.RH = H - run;
+        for (int b = 0; b < a.RH; b++) a.rhigh[b] = uint8_t(st.high[run + b]);
+        std::vector<int> qpos;
+        for (int q = 0; q < st.L; q++) qpos.push_back(q);
+        for (int q : st.high) qpos.push_back(q);
+        std::sort(qpos.begin(), qpos.end());
+        a.outer.npos = int(qpos.size());
+        for (size_t i = 0; i < qpos.size(); i++) a.outer.pos[i] = uint8_t(qpos[i]);
+        a.nops = L.count;
+        a.nrot = L.nrot;
+        for (int r = 0; r < L.nrot; r++) a.slot[r] = L.slot[r];
+        const size_t smem = 2 * (sizeof(T) << st.T) + size_t(a.nrot) * (kAdjThreads / 32) * 8 + (8u << a.RH);
+        k_adj_stage<T><<<grid, kAdjThreads, smem, s>>>((T*)state, (T*)lam, ntiles, a, dops + L.first, part);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            rc = fail(e, "reverse-sweep stage", msg);
+            break;
+        }
+        note_launches(1);
+    }
+    if (dops) cudaFreeAsync(dops, s);
+    return rc;
+}
+
 int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gate* gates, size_t m,
                      const double* params, size_t np, const qs_pauli_term* terms, size_t nt, cudaStream_t s, int sms,
                      double* energy, double* grad, size_t* err, std::string* msg) {
@@ -354,7 +645,9 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
     std::vector<PauliDev> ht = pauli_table(terms, nt);
     const size_t amp = prec == QS_PREC_C64 ? 8 : 16;
     const uint64_t N = 1ull << n;
-    const int pgrid = grid_for_pairs(N >> 1, sms);
+    const bool tiled = n >= kAdjT;  // forward as fused stages, reverse sweep as tiled stages
+    const int pgrid = tiled ? (prec == QS_PREC_C64 ? adj_grid<float2>(n, sms) : adj_grid<double2>(n, sms))
+                            : grid_for_pairs(N >> 1, sms);
     auto al = [](size_t x) { return ((x + 255) / 256) * 256; };
     const size_t o_cs = 0, o_terms = o_cs + al(cs.size() * 16), o_part = o_terms + al(nt * sizeof(PauliDev) + 1),
                  o_res = o_part + al(size_t(std::max(nrot, 1)) * pgrid * 8 + 4096 * 16),
@@ -374,7 +667,20 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
                      "terms upload");
         AJ_CHECK(cudaMemcpyAsync(blob + o_save, state, N * amp, cudaMemcpyDeviceToDevice, s), "save state");
         // forward
-        for (size_t g = 0; g < m; g++) {
+        if (tiled) {
+            std::vector<OpDesc> fops(m);
+            for (size_t g = 0; g < m; g++) {
+                if (rot_slot[g] >= 0) {
+                    const std::vector<double> R = rotation_matrix(gates[g].kind, cs[g].x, cs[g].y);
+                    classify_gate(R.data(), 1, gates[g].targets, &fops[g]);
+                } else {
+                    fops[g] = fwd[g];
+                }
+            }
+            const qs_circuit_options fo{1, 5, 0, 0};
+            if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg)) != QS_OK) goto done;
+        }
+        for (size_t g = 0; g < m && !tiled; g++) {
             if (rot_slot[g] >= 0) {
                 if (prec == QS_PREC_C64)
                     launch_rot<float2>(gates[g].kind, state, n, int(gates[g].targets[0]), dcs, int(g), 0, s, sms);
@@ -394,7 +700,15 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
         if (inner_product(state, prec, lam, prec, n, s, sms, part + size_t(std::max(nrot, 1)) * pgrid, dres))
             AJ_CHECK(cudaGetLastError(), "energy");
         // reverse
-        for (size_t gg = m; gg-- > 0;) {
+        if (tiled) {
+            rc = prec == QS_PREC_C64
+                     ? reverse_tiled<float2>(state, lam, n, prec, arith, gates, m, params, rot_slot, inv, part, pgrid,
+                                             s, sms, msg)
+                     : reverse_tiled<double2>(state, lam, n, prec, arith, gates, m, params, rot_slot, inv, part,
+                                              pgrid, s, sms, msg);
+            if (rc != QS_OK) goto done;
+        }
+        for (size_t gg = m; gg-- > 0 && !tiled;) {
             if (rot_slot[gg] >= 0) {
                 double* p = part + size_t(rot_slot[gg]) * pgrid;
                 if (prec == QS_PREC_C64)

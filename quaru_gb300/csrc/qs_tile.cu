@@ -57,14 +57,6 @@ struct TileElem<3> {
     using T = float2;
 };
 
-__device__ __forceinline__ uint32_t expand_local(uint32_t t, const uint8_t* pos, int npos) {
-    for (int i = 0; i < npos; i++) {
-        const uint32_t p = pos[i];
-        t = ((t >> p) << (p + 1)) | (t & ((1u << p) - 1u));
-    }
-    return t;
-}
-
 // ---- load / store conversions
 template <int REP>
 __device__ __forceinline__ typename TileElem<REP>::T tile_load(const void* st, uint64_t g);
@@ -151,22 +143,6 @@ __device__ __forceinline__ float4 phase_mul(const double* p, float4 x, int) {
         df_dot_pair<2>(uh, ul, xh, xl, r.z, r.w);
     }
     return r;
-}
-
-// Expanded tuple index of tuple t (local fixed bits' values ORed in).
-__device__ __forceinline__ uint32_t tuple_index(uint32_t t, int npos, const uint32_t (&seg)[5], const uint8_t* pos,
-                                                uint32_t fixval) {
-    uint32_t e;
-    if (npos <= 4) {
-        e = t & seg[0];
-        if (npos > 0) e |= (t << 1) & seg[1];
-        if (npos > 1) e |= (t << 2) & seg[2];
-        if (npos > 2) e |= (t << 3) & seg[3];
-        if (npos > 3) e |= (t << 4) & seg[4];
-    } else {
-        e = expand_local(t, pos, npos);
-    }
-    return e | fixval;
 }
 
 template <int REP>

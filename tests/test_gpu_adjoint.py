@@ -99,6 +99,54 @@ def test_adjoint_matches_finite_differences_and_shift(n, layers):
         assert abs(grad[p] - ps) < 1e-9, (p, grad[p], ps)
 
 
+@pytest.mark.parametrize("n,precision", [(11, 0), (13, 0), (12, 1)])
+def test_adjoint_tiled_mixed_gates(n, precision):
+    """n >= 11: forward as fused stages and the reverse sweep as tiled stages. RX/RY/RZ mixed with
+    fixed gates of every kind the tiles hold (H, S, CZ, CNOT, Toffoli, controlled rotation) and one
+    they do not (a dense 2-qubit unitary: its own sweeps), one parameter shared by three rotations;
+    every parameter against central differences, and against parameter shift where that is exact."""
+    import quaru_gb300 as q
+    from quaru_gb300 import operation as O
+    from quaru_gb300.register import ParamGate
+    from quaru_gb300.workloads import SplitMix64, chain_hamiltonian
+
+    rng = SplitMix64(500 + n)
+    nrng = np.random.default_rng(n)
+    gates, npar = [], 0
+    for layer in range(3):
+        for qb in range(n):
+            k = (qb + layer) % 3
+            mk = (ParamGate.rx, ParamGate.ry, ParamGate.rz)[k]
+            gates.append(mk(qb, npar))
+            npar += 1
+        a, b, c = (int(x) for x in nrng.permutation(n)[:3])
+        gates += [ParamGate.fixed(O.hadamard(a)), ParamGate.fixed(O.phase(b)), ParamGate.fixed(O.cnz([a], b)),
+                  ParamGate.fixed(O.cnot(b, c)), ParamGate.fixed(O.cnx([a, b], c)),
+                  ParamGate.fixed(O.to_controlled(O.Operation(np.array([[0.6, 0.8j], [0.8j, 0.6]]), [c]), a))]
+        z = nrng.normal(size=(4, 4)) + 1j * nrng.normal(size=(4, 4))
+        gates.append(ParamGate.fixed(O.Operation(np.linalg.qr(z)[0], [a, c])))
+    shared = npar  # one parameter used by three rotations: its gradient is their sum
+    gates += [ParamGate.ry(0, shared), ParamGate.rx(n // 2, shared), ParamGate.rz(n - 1, shared)]
+    npar += 1
+    params = np.array([2 * math.pi * rng.uniform() for _ in range(npar)])
+    terms = chain_hamiltonian(n, rng) + [(0.3, 0b101, 0b100)]
+    reg = q.Register.from_int(n, 0, precision=precision)
+    before = reg.state
+    e, grad = reg.adjoint_gradient(gates, params, terms)
+    assert np.array_equal(reg.state, before)
+    tol_ps, tol_fd = (1e-9, 1e-6) if precision == 0 else (2e-4, 2e-4)
+    for p in range(npar):
+        pp, pm = params.copy(), params.copy()
+        if p != shared:  # the shift rule is exact for a parameter of a single rotation
+            pp[p] += math.pi / 2
+            pm[p] -= math.pi / 2
+            ps = (energy_gpu(q, n, gates, pp, terms) - energy_gpu(q, n, gates, pm, terms)) / 2
+            assert abs(grad[p] - ps) < tol_ps, (p, grad[p], ps)
+        pp[p], pm[p] = params[p] + 1e-6, params[p] - 1e-6
+        fd = (energy_gpu(q, n, gates, pp, terms) - energy_gpu(q, n, gates, pm, terms)) / 2e-6
+        assert abs(grad[p] - fd) < tol_fd, (p, grad[p], fd)
+
+
 def test_adjoint_config4_size_fp64_and_mixed():
     """20 qubits, 10 layers, 400 parameters: spot-check 6 parameters by parameter shift and central
     differences; the complex64 (mixed) gradient agrees with FP64 to 1e-4 and its state has 1 - F <= 1e-6."""
