@@ -414,7 +414,8 @@ def precision_section(q, torch, args) -> dict:
 
 def adjoint_section(q, torch, args) -> dict:
     """Gradient throughput on the 20-qubit, 10-layer ansatz (400 parameters, ZZ + X chain observable):
-    FP64 (complex128) vs mixed (complex64 state, FP64-accurate accumulations), and the mixed run's 1 - F."""
+    FP64 (complex128, FP64 FMA arithmetic), complex128 with double-float arithmetic, and mixed (complex64
+    state, FP64 accumulations), with the mixed run's 1 - F."""
     from quaru_gb300.workloads import config4
 
     gates, params, terms = config4()
@@ -422,9 +423,10 @@ def adjoint_section(q, torch, args) -> dict:
     out = {"workload": "20-qubit hardware-efficient ansatz, 10 layers (RY, RZ on every qubit + CNOT ladder), "
                        "400 parameters, H = sum a_i Z_i Z_i+1 + sum b_i X_i"}
     grads = {}
-    for name, prec in (("fp64", q.QS_PREC_C128), ("mixed", q.QS_PREC_C64)):
+    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("fp64_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
+                              ("mixed", q.QS_PREC_C64, q.QS_ARITH_FMA)):
         reg = q.Register.from_int(n, 0, precision=prec)
-        reg.set_arith(q.QS_ARITH_FMA)
+        reg.set_arith(arith)
         for _ in range(3):
             e, g = reg.adjoint_gradient(gates, params, terms)
         reps = 5
@@ -435,6 +437,7 @@ def adjoint_section(q, torch, args) -> dict:
         grads[name] = g
         out[name] = {"ms_per_gradient": 1e3 * dt, "grads_per_s": len(params) / dt, "energy": e}
     out["mixed_vs_fp64_speedup"] = out["fp64"]["ms_per_gradient"] / out["mixed"]["ms_per_gradient"]
+    out["max_grad_diff_df64_vs_fp64"] = float(np.max(np.abs(grads["fp64_df64"] - grads["fp64"])))
     out["max_grad_diff_mixed_vs_fp64"] = float(np.max(np.abs(grads["mixed"] - grads["fp64"])))
     a = q.Register.from_int(n, 0)
     a.set_arith(q.QS_ARITH_FMA)

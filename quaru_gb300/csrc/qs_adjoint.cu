@@ -295,15 +295,126 @@ __device__ __forceinline__ double adj_rot_tile(T* sp, T* sl, const AdjOpDev& op,
     return acc;
 }
 
-template <typename T>
+// ---- double-float reverse-sweep tiles (complex128 registers with QS_ARITH_DF64): amplitudes held as
+// float4 (re_hi, re_lo, im_hi, im_lo), split once on load and joined once on store. Rotations run on
+// the FP32 pipe (df_dot_pair); each pair's Im<lambda|A|psi> is a double-float dot product rounded
+// once to FP64 (df_dot) and accumulated in FP64. Fixed gates in these stages are pure moves.
+template <int AXIS>
+__device__ __forceinline__ double adj_im_df(float4 l0, float4 l1, float4 a, float4 b) {
+    // terms u * x of Im<lambda|A|psi> (see im_term): u from lambda, x from psi
+    float uh[4], ul[4], xh[4], xl[4];
+    auto set = [&](int k, float vh, float vl, float wh, float wl, bool neg) {
+        uh[k] = neg ? -vh : vh;
+        ul[k] = neg ? -vl : vl;
+        xh[k] = wh;
+        xl[k] = wl;
+    };
+    if (AXIS == QS_GATE_RX) {  // l0.re*b.im - l0.im*b.re + l1.re*a.im - l1.im*a.re
+        set(0, l0.x, l0.y, b.z, b.w, false); set(1, l0.z, l0.w, b.x, b.y, true);
+        set(2, l1.x, l1.y, a.z, a.w, false); set(3, l1.z, l1.w, a.x, a.y, true);
+    } else if (AXIS == QS_GATE_RY) {  // l1.re*a.re + l1.im*a.im - l0.re*b.re - l0.im*b.im
+        set(0, l1.x, l1.y, a.x, a.y, false); set(1, l1.z, l1.w, a.z, a.w, false);
+        set(2, l0.x, l0.y, b.x, b.y, true); set(3, l0.z, l0.w, b.z, b.w, true);
+    } else {  // l0.re*a.im - l0.im*a.re - l1.re*b.im + l1.im*b.re
+        set(0, l0.x, l0.y, a.z, a.w, false); set(1, l0.z, l0.w, a.x, a.y, true);
+        set(2, l1.x, l1.y, b.z, b.w, true); set(3, l1.z, l1.w, b.x, b.y, false);
+    }
+    return df_dot<4>(uh, ul, xh, xl);
+}
+
+// c * p + q2 * r in double-float: the rot_pair formulas with (c, s) = (ch + cl, sh + sl).
+__device__ __forceinline__ void df_lin2(float ch, float cl, float p_h, float p_l, float dh, float dl, float q_h,
+                                        float q_l, float& oh, float& ol) {
+    const float uh[2] = {ch, dh}, ul[2] = {cl, dl}, xh[2] = {p_h, q_h}, xl[2] = {p_l, q_l};
+    df_dot_pair<2>(uh, ul, xh, xl, oh, ol);
+}
+
+template <int AXIS>
+__device__ __forceinline__ void df_rot_pair(float ch, float cl, float sh, float sl, float4& a, float4& b) {
+    float4 na, nb;
+    if (AXIS == QS_GATE_RY) {  // [[c, -s], [s, c]]
+        df_lin2(ch, cl, a.x, a.y, -sh, -sl, b.x, b.y, na.x, na.y);
+        df_lin2(ch, cl, a.z, a.w, -sh, -sl, b.z, b.w, na.z, na.w);
+        df_lin2(sh, sl, a.x, a.y, ch, cl, b.x, b.y, nb.x, nb.y);
+        df_lin2(sh, sl, a.z, a.w, ch, cl, b.z, b.w, nb.z, nb.w);
+    } else if (AXIS == QS_GATE_RZ) {  // diag(c - i s, c + i s)
+        df_lin2(ch, cl, a.x, a.y, sh, sl, a.z, a.w, na.x, na.y);
+        df_lin2(ch, cl, a.z, a.w, -sh, -sl, a.x, a.y, na.z, na.w);
+        df_lin2(ch, cl, b.x, b.y, -sh, -sl, b.z, b.w, nb.x, nb.y);
+        df_lin2(ch, cl, b.z, b.w, sh, sl, b.x, b.y, nb.z, nb.w);
+    } else {  // RX: [[c, -i s], [-i s, c]]
+        df_lin2(ch, cl, a.x, a.y, sh, sl, b.z, b.w, na.x, na.y);
+        df_lin2(ch, cl, a.z, a.w, -sh, -sl, b.x, b.y, na.z, na.w);
+        df_lin2(ch, cl, b.x, b.y, sh, sl, a.z, a.w, nb.x, nb.y);
+        df_lin2(ch, cl, b.z, b.w, -sh, -sl, a.x, a.y, nb.z, nb.w);
+    }
+    a = na;
+    b = nb;
+}
+
+template <int AXIS>
+__device__ __forceinline__ double adj_rot_tile_df(float4* sp, float4* sl, const AdjOpDev& op, uint32_t tsize) {
+    const TileOp& t = op.t;
+    uint32_t seg[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) seg[j] = t.seg[j];
+    const uint32_t tb = 1u << t.tb[0];
+    float ch, cl, sh, sl_;
+    df_split(op.c, ch, cl);
+    df_split(op.s, sh, sl_);
+    double acc = 0.0;
+    for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += kAdjThreads) {
+        const uint32_t i0 = tuple_index(p, t.npos, seg, t.pos, 0u), i1 = i0 | tb;
+        float4 a = sp[i0], b = sp[i1], l0 = sl[i0], l1 = sl[i1];
+        acc += adj_im_df<AXIS>(l0, l1, a, b);
+        df_rot_pair<AXIS>(ch, cl, sh, sl_, a, b);
+        df_rot_pair<AXIS>(ch, cl, sh, sl_, l0, l1);
+        sp[i0] = a;
+        sp[i1] = b;
+        sl[i0] = l0;
+        sl[i1] = l1;
+    }
+    return acc;
+}
+
+// pure moves (permutations with factors 1, -1, i, -i) on double-float amplitudes
+__device__ __forceinline__ float4 df_pf(float4 x, uint8_t c) {
+    if (c == 1) return make_float4(-x.x, -x.y, -x.z, -x.w);
+    if (c == 2) return make_float4(-x.z, -x.w, x.x, x.y);
+    if (c == 3) return make_float4(x.z, x.w, -x.x, -x.y);
+    return x;
+}
+
+__device__ __forceinline__ void adj_move_df(float4* s, const TileOp& op, uint32_t tsize) {
+    const uint32_t ntup = tsize >> op.npos;
+    uint32_t seg[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) seg[j] = op.seg[j];
+    const int D = 1 << op.k;
+    for (uint32_t p = threadIdx.x; p < ntup; p += kAdjThreads) {
+        const uint32_t i0 = tuple_index(p, op.npos, seg, op.pos, op.lfixval);
+        float4 y[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+            if (r < D && op.pf[r] != PF_SKIP_DEV) y[r] = s[i0 + op.offsrc[r]];
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+            if (r < D && op.pf[r] != PF_SKIP_DEV) s[i0 + op.off[r]] = df_pf(y[r], op.pf[r]);
+    }
+}
+
+template <typename T, bool DF>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, T* __restrict__ lam, uint64_t ntiles,
                                                            const __grid_constant__ AdjStageArgs a,
                                                            const AdjOpDev* __restrict__ ops,
                                                            double* __restrict__ partials) {
+    static_assert(!DF || sizeof(T) == 16, "double-float tiles hold complex128 registers");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t tsize = 1u << a.T;
     T* sp = reinterpret_cast<T*>(smem_raw);
     T* sl = sp + tsize;
+    float4* fp = reinterpret_cast<float4*>(sp);  // the same buffers as double-float amplitudes
+    float4* fl = reinterpret_cast<float4*>(sl);
     double* sacc = reinterpret_cast<double*>(sl + tsize);  // [nrot][8 warps]
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(sacc + size_t(a.nrot) * (kAdjThreads / 32));
     const int nrows = 1 << a.RH, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -320,8 +431,19 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
         const uint64_t base = expand_index(tile, a.outer);
         for (uint32_t i = threadIdx.x; i < tsize; i += kAdjThreads) {
             const uint64_t g = base + rowoff[i >> a.RL] + (i & rmask);
-            sp[i] = psi[g];
-            sl[i] = lam[g];
+            if constexpr (DF) {
+                const double2 v = reinterpret_cast<const double2*>(psi)[g], w = reinterpret_cast<const double2*>(lam)[g];
+                float4 f;
+                df_split(v.x, f.x, f.y);
+                df_split(v.y, f.z, f.w);
+                fp[i] = f;
+                df_split(w.x, f.x, f.y);
+                df_split(w.y, f.z, f.w);
+                fl[i] = f;
+            } else {
+                sp[i] = psi[g];
+                sl[i] = lam[g];
+            }
         }
         __syncthreads();
         for (int o = 0; o < a.nops; o++) {
@@ -329,15 +451,27 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
             if ((base & op.t.omask) != op.t.oval) continue;  // the same for the whole block
             if (op.rot >= 0) {
                 double v;
-                if (op.axis == QS_GATE_RX)
-                    v = adj_rot_tile<T, QS_GATE_RX>(sp, sl, op, tsize);
-                else if (op.axis == QS_GATE_RY)
-                    v = adj_rot_tile<T, QS_GATE_RY>(sp, sl, op, tsize);
-                else
-                    v = adj_rot_tile<T, QS_GATE_RZ>(sp, sl, op, tsize);
+                if constexpr (DF) {
+                    if (op.axis == QS_GATE_RX)
+                        v = adj_rot_tile_df<QS_GATE_RX>(fp, fl, op, tsize);
+                    else if (op.axis == QS_GATE_RY)
+                        v = adj_rot_tile_df<QS_GATE_RY>(fp, fl, op, tsize);
+                    else
+                        v = adj_rot_tile_df<QS_GATE_RZ>(fp, fl, op, tsize);
+                } else {
+                    if (op.axis == QS_GATE_RX)
+                        v = adj_rot_tile<T, QS_GATE_RX>(sp, sl, op, tsize);
+                    else if (op.axis == QS_GATE_RY)
+                        v = adj_rot_tile<T, QS_GATE_RY>(sp, sl, op, tsize);
+                    else
+                        v = adj_rot_tile<T, QS_GATE_RZ>(sp, sl, op, tsize);
+                }
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
                 if (lane == 0) sacc[op.rot * (kAdjThreads / 32) + warp] += v;
+            } else if constexpr (DF) {
+                adj_move_df(fp, op.t, tsize);
+                adj_move_df(fl, op.t, tsize);
             } else {
                 adj_fixed(sp, op.t, tsize);
                 adj_fixed(sl, op.t, tsize);
@@ -346,8 +480,16 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
         }
         for (uint32_t i = threadIdx.x; i < tsize; i += kAdjThreads) {
             const uint64_t g = base + rowoff[i >> a.RL] + (i & rmask);
-            psi[g] = sp[i];
-            lam[g] = sl[i];
+            if constexpr (DF) {
+                const float4 f = fp[i], h = fl[i];
+                reinterpret_cast<double2*>(psi)[g] =
+                    make_double2(__dadd_rn(df_f2d(f.x), df_f2d(f.y)), __dadd_rn(df_f2d(f.z), df_f2d(f.w)));
+                reinterpret_cast<double2*>(lam)[g] =
+                    make_double2(__dadd_rn(df_f2d(h.x), df_f2d(h.y)), __dadd_rn(df_f2d(h.z), df_f2d(h.w)));
+            } else {
+                psi[g] = sp[i];
+                lam[g] = sl[i];
+            }
         }
         __syncthreads();
     }
@@ -472,9 +614,19 @@ static std::vector<double> rotation_matrix(int axis, double c, double s) {
 template <typename T>
 static int adj_grid(int n, int sms) {
     const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 + (8u << 6);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_adj_stage<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<T>, kAdjThreads, smem);
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_adj_stage<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (sizeof(T) == 16)
+            cudaFuncSetAttribute(k_adj_stage<T, sizeof(T) == 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem));
+    }
+    int per_sm = 1;  // the smaller of the two variants' occupancies
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<T, false>, kAdjThreads, smem);
+    if (sizeof(T) == 16) {
+        int df = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&df, k_adj_stage<T, sizeof(T) == 16>, kAdjThreads, smem);
+        per_sm = std::min(per_sm, df);
+    }
     const uint64_t ntiles = 1ull << (n - kAdjT);
     return int(std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm))));
 }
@@ -507,25 +659,27 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
     struct Launch {
         int stage, first, count, nrot;
         int slot[kAdjMaxRot];
+        bool moves_only;  // every fixed gate a pure move (double-float tiles can take the launch)
     };
     std::vector<Launch> launches;
     for (size_t si = 0; si < stages.size(); si++) {
         const TileStage& st = stages[si];
         if (!st.tiled) {
-            launches.push_back(Launch{int(si), -1, 0, 0, {}});
+            launches.push_back(Launch{int(si), -1, 0, 0, {}, false});
             continue;
         }
-        Launch cur{int(si), int(host.size()), 0, 0, {}};
+        Launch cur{int(si), int(host.size()), 0, 0, {}, true};
         for (int idx : st.ops) {
             const int g = src[idx];
             if (rot_slot[g] >= 0 && cur.nrot == kAdjMaxRot) {
                 launches.push_back(cur);
-                cur = Launch{int(si), int(host.size()), 0, 0, {}};
+                cur = Launch{int(si), int(host.size()), 0, 0, {}, true};
             }
             AdjOpDev e;
             std::memset(&e, 0, sizeof(e));
             e.t = make_tile_op(rops[idx], st);
             e.rot = -1;
+            if (rot_slot[g] < 0 && rops[idx].kind != OP_MONO_PF) cur.moves_only = false;
             if (rot_slot[g] >= 0) {
                 const double th = params[gates[g].param];
                 e.rot = cur.nrot;
@@ -575,7 +729,12 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
         a.nrot = L.nrot;
         for (int r = 0; r < L.nrot; r++) a.slot[r] = L.slot[r];
         const size_t smem = 2 * (sizeof(T) << st.T) + size_t(a.nrot) * (kAdjThreads / 32) * 8 + (8u << a.RH);
-        k_adj_stage<T><<<grid, kAdjThreads, smem, s>>>((T*)state, (T*)lam, ntiles, a, dops + L.first, part);
+        if (sizeof(T) == 16 && L.moves_only && arith == QS_ARITH_DF64)
+            k_adj_stage<T, sizeof(T) == 16><<<grid, kAdjThreads, smem, s>>>((T*)state, (T*)lam, ntiles, a,
+                                                                           dops + L.first, part);
+        else
+            k_adj_stage<T, false><<<grid, kAdjThreads, smem, s>>>((T*)state, (T*)lam, ntiles, a, dops + L.first,
+                                                                  part);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             rc = fail(e, "reverse-sweep stage", msg);

@@ -99,12 +99,13 @@ def test_adjoint_matches_finite_differences_and_shift(n, layers):
         assert abs(grad[p] - ps) < 1e-9, (p, grad[p], ps)
 
 
-@pytest.mark.parametrize("n,precision", [(11, 0), (13, 0), (12, 1)])
-def test_adjoint_tiled_mixed_gates(n, precision):
+@pytest.mark.parametrize("n,precision,arith", [(11, 0, 1), (13, 0, 1), (12, 1, 1), (12, 0, 2), (14, 0, 2)])
+def test_adjoint_tiled_mixed_gates(n, precision, arith):
     """n >= 11: forward as fused stages and the reverse sweep as tiled stages. RX/RY/RZ mixed with
     fixed gates of every kind the tiles hold (H, S, CZ, CNOT, Toffoli, controlled rotation) and one
     they do not (a dense 2-qubit unitary: its own sweeps), one parameter shared by three rotations;
-    every parameter against central differences, and against parameter shift where that is exact."""
+    every parameter against central differences, and against parameter shift where that is exact.
+    arith = 2 (DF64) runs the stages whose fixed gates are pure moves in double-float tiles."""
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.register import ParamGate
@@ -131,6 +132,7 @@ def test_adjoint_tiled_mixed_gates(n, precision):
     params = np.array([2 * math.pi * rng.uniform() for _ in range(npar)])
     terms = chain_hamiltonian(n, rng) + [(0.3, 0b101, 0b100)]
     reg = q.Register.from_int(n, 0, precision=precision)
+    reg.set_arith(arith)
     before = reg.state
     e, grad = reg.adjoint_gradient(gates, params, terms)
     assert np.array_equal(reg.state, before)
