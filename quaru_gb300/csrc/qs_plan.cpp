@@ -63,7 +63,7 @@ std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, 
             uint64_t need = 0;
             for (int j = 0; j < op.k; j++) need |= 1ull << op.tq[j];
             need &= ~low_mask;
-            if (tileable(op) && __builtin_popcountll(high | need) <= H) {
+            if (tileable(op) && __builtin_popcountll(high | need) <= H && st.ops.size() < size_t(kMaxStageOps)) {
                 high |= need;
                 st.ops.push_back(idx);
             } else {

@@ -17,6 +17,7 @@
 namespace qs {
 
 constexpr int kTileMaxHigh = 8;
+constexpr int kMaxStageOps = 64;       // gates per stage: the stage's op table lives in shared memory
 constexpr int kPassBits = 4;           // register bits of a pass: 16 amplitudes per thread
 constexpr int kLaneBits = 4;           // tile bits 0..3 live on the lanes of a warp during a pass
 constexpr int kPassMinT = 9;           // passes need whole warps of tuples: 2^(T-4) >= 32

@@ -114,6 +114,24 @@ def test_fused_c64_register_passes_full_gate_set(n, tile):
     assert floored_rel_err(g.state, h.state) <= 2e-5
 
 
+@pytest.mark.parametrize("n,precision", [(9, 0), (11, 0), (12, 1), (11, 1)])
+def test_fused_deep_circuit_on_a_single_tile(n, precision):
+    """A circuit whose every gate fits one tile (n <= T): stages are capped in length, so the op
+    tables stay within shared memory; results equal the gate-by-gate run."""
+    import quaru_gb300 as q
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    ops = flatten(layered_circuit(n, 30, 31 + n))  # 30 layers: > 600 gates
+    a = q.Register.from_int(n, 0, precision=precision)
+    a.apply_gates(ops, fuse=0)
+    b = q.Register.from_int(n, 0, precision=precision)
+    b.apply_gates(ops, fuse=1)
+    if precision == 0:
+        assert value_equal(a.state, b.state)
+    else:
+        assert floored_rel_err(b.state, a.state) <= 5e-5
+
+
 def test_fused_large_state_permutation_round_trip_bit_exact():
     """24 qubits: a permutation-and-phase circuit followed by its inverse restores the state exactly."""
     import quaru_gb300 as q
