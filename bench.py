@@ -451,8 +451,8 @@ def adjoint_section(q, torch, args) -> dict:
 
 
 def batch_section(q, args) -> dict:
-    """256 ansatz circuits (10..22 qubits, 4..12 layers): one persistent graph replay per run vs a loop of
-    single-circuit adjoint calls."""
+    """256 ansatz circuits (10..22 qubits, 4..12 layers): one persistent graph replay per run (FP64,
+    complex128 with double-float tiles, complex64) vs a loop of single-circuit adjoint calls (FP64)."""
     from quaru_gb300.batch import Batch
     from quaru_gb300.workloads import config5
 
@@ -461,9 +461,10 @@ def batch_section(q, args) -> dict:
     ngrads = len(params)
     out = {"workload": "256 ansatz circuits, qubits ~ U{10..22}, layers ~ U{4..12}, random Z/ZZ/X observables",
            "circuits": len(circuits), "parameters": ngrads}
-    for name, prec in (("fp64", q.QS_PREC_C128), ("mixed", q.QS_PREC_C64)):
+    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("fp64_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
+                              ("mixed", q.QS_PREC_C64, q.QS_ARITH_FMA)):
         t0 = time.perf_counter()
-        b = Batch(circuits, precision=prec)
+        b = Batch(circuits, precision=prec, arith=arith)
         setup = time.perf_counter() - t0
         b.run(params)
         reps = 3

@@ -224,7 +224,8 @@ typedef struct qs_batch_options {
     int precision;       /* QS_PREC_C128 or QS_PREC_C64 */
     int chunk_log2;      /* amplitude pairs per work item = 2^chunk_log2; 0 = autotune */
     int ctas_per_sm;     /* persistent CTAs per SM; 0 = autotune */
-    int reserved;
+    int arith;           /* QS_ARITH_DF64: complex128 stages of rotations and CNOTs in double-float
+                            tiles; any other value: FP64 arithmetic */
 } qs_batch_options;
 
 typedef struct qs_batch qs_batch;

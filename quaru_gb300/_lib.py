@@ -69,7 +69,7 @@ class QsBatchCircuit(ctypes.Structure):
 
 class QsBatchOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("chunk_log2", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("arith", ctypes.c_int)]
 
 SIGNATURES = {
     "qs_register_new": (_i, [_P(ctypes.c_uint8), _sz, _i, _P(_vp)]),

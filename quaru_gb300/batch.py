@@ -12,7 +12,8 @@ from .register import EngineError, OperationError, ParamGate, _check, _dp, _paul
 class Batch:
     """Circuits (ParamGate lists, parameter counts, Pauli observables) prepared once; run() replays the graph."""
 
-    def __init__(self, circuits, precision: int = _lib.QS_PREC_C128, chunk_log2: int = 0, ctas_per_sm: int = 0):
+    def __init__(self, circuits, precision: int = _lib.QS_PREC_C128, chunk_log2: int = 0, ctas_per_sm: int = 0,
+                 arith: int = _lib.QS_ARITH_FMA):
         lib = _lib.load()
         self._keep = []
         arr = (_lib.QsBatchCircuit * max(1, len(circuits)))()
@@ -37,7 +38,7 @@ class Batch:
             arr[i].n, arr[i].gates, arr[i].m = n, cg, len(gates)
             arr[i].nparams, arr[i].terms, arr[i].nterms = nparams, pt, len(terms)
             self.nparams.append(nparams)
-        opts = _lib.QsBatchOptions(precision, chunk_log2, ctas_per_sm, 0)
+        opts = _lib.QsBatchOptions(precision, chunk_log2, ctas_per_sm, arith)
         h = ctypes.c_void_p()
         err = np.zeros(3, dtype=np.uintp)
         _check(lib.qs_batch_create(arr, len(circuits), ctypes.byref(opts), ctypes.byref(h), _sp(err)), err)

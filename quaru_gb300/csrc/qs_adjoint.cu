@@ -20,6 +20,7 @@
 #include "qs_device.cuh"
 #include "qs_kernels.h"
 #include "qs_pass.cuh"
+#include "qs_rot.cuh"
 #include "qs_reduce.cuh"
 #include "qs_tile.h"
 
@@ -100,25 +101,6 @@ __global__ void __launch_bounds__(kAT) k_pauli_sum(const T* __restrict__ psi, T*
     }
 }
 
-// ---------------------------------------------------------------- rotations
-// R_A(theta) = cos(theta/2) I - i sin(theta/2) A on the pair (a, b) = (bit 0, bit 1).
-template <int AXIS, typename R>
-__device__ __forceinline__ void rot_pair(R c, R s, R& ax, R& ay, R& bx, R& by) {
-    if (AXIS == QS_GATE_RY) {  // [[c, -s], [s, c]]
-        const R nax = c * ax - s * bx, nay = c * ay - s * by;
-        const R nbx = s * ax + c * bx, nby = s * ay + c * by;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    } else if (AXIS == QS_GATE_RZ) {  // diag(c - i s, c + i s)
-        const R nax = c * ax + s * ay, nay = c * ay - s * ax;
-        const R nbx = c * bx - s * by, nby = c * by + s * bx;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    } else {  // RX: [[c, -i s], [-i s, c]]
-        const R nax = c * ax + s * by, nay = c * ay - s * bx;
-        const R nbx = c * bx + s * ay, nby = c * by - s * ax;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    }
-}
-
 template <typename T, int AXIS>
 __global__ void __launch_bounds__(kAT) k_rot(T* __restrict__ psi, uint64_t npairs, int q,
                                              const double2* __restrict__ cs, int slot, int inverse) {
@@ -132,25 +114,6 @@ __global__ void __launch_bounds__(kAT) k_rot(T* __restrict__ psi, uint64_t npair
         rot_pair<AXIS>(c, s, a.x, a.y, b.x, b.y);
         psi[i0] = a;
         psi[i0 | tb] = b;
-    }
-}
-
-// Im<lambda|A|psi> over the pairs of qubit q, then psi, lambda <- R_A(-theta) psi, lambda.
-template <int AXIS>
-__device__ __forceinline__ double im_term(double2 l0, double2 l1, double2 a, double2 b) {
-    if (AXIS == QS_GATE_RX) return (l0.x * b.y - l0.y * b.x) + (l1.x * a.y - l1.y * a.x);
-    if (AXIS == QS_GATE_RY) return (l1.x * a.x + l1.y * a.y) - (l0.x * b.x + l0.y * b.y);
-    return (l0.x * a.y - l0.y * a.x) - (l1.x * b.y - l1.y * b.x);
-}
-
-template <int AXIS>
-__device__ __forceinline__ void im_term_acc(DfAcc& acc, float2 l0, float2 l1, float2 a, float2 b) {
-    if (AXIS == QS_GATE_RX) {
-        acc.add_prod(l0.x, b.y); acc.sub_prod(l0.y, b.x); acc.add_prod(l1.x, a.y); acc.sub_prod(l1.y, a.x);
-    } else if (AXIS == QS_GATE_RY) {
-        acc.add_prod(l1.x, a.x); acc.add_prod(l1.y, a.y); acc.sub_prod(l0.x, b.x); acc.sub_prod(l0.y, b.y);
-    } else {
-        acc.add_prod(l0.x, a.y); acc.sub_prod(l0.y, a.x); acc.sub_prod(l1.x, b.y); acc.add_prod(l1.y, b.x);
     }
 }
 
@@ -293,63 +256,6 @@ __device__ __forceinline__ double adj_rot_tile(T* sp, T* sl, const AdjOpDev& op,
     }
     if constexpr (sizeof(R) == 4) acc = __dadd_rn(df_f2d(facc.s), df_f2d(facc.c));
     return acc;
-}
-
-// ---- double-float reverse-sweep tiles (complex128 registers with QS_ARITH_DF64): amplitudes held as
-// float4 (re_hi, re_lo, im_hi, im_lo), split once on load and joined once on store. Rotations run on
-// the FP32 pipe (df_dot_pair); each pair's Im<lambda|A|psi> is a double-float dot product rounded
-// once to FP64 (df_dot) and accumulated in FP64. Fixed gates in these stages are pure moves.
-template <int AXIS>
-__device__ __forceinline__ double adj_im_df(float4 l0, float4 l1, float4 a, float4 b) {
-    // terms u * x of Im<lambda|A|psi> (see im_term): u from lambda, x from psi
-    float uh[4], ul[4], xh[4], xl[4];
-    auto set = [&](int k, float vh, float vl, float wh, float wl, bool neg) {
-        uh[k] = neg ? -vh : vh;
-        ul[k] = neg ? -vl : vl;
-        xh[k] = wh;
-        xl[k] = wl;
-    };
-    if (AXIS == QS_GATE_RX) {  // l0.re*b.im - l0.im*b.re + l1.re*a.im - l1.im*a.re
-        set(0, l0.x, l0.y, b.z, b.w, false); set(1, l0.z, l0.w, b.x, b.y, true);
-        set(2, l1.x, l1.y, a.z, a.w, false); set(3, l1.z, l1.w, a.x, a.y, true);
-    } else if (AXIS == QS_GATE_RY) {  // l1.re*a.re + l1.im*a.im - l0.re*b.re - l0.im*b.im
-        set(0, l1.x, l1.y, a.x, a.y, false); set(1, l1.z, l1.w, a.z, a.w, false);
-        set(2, l0.x, l0.y, b.x, b.y, true); set(3, l0.z, l0.w, b.z, b.w, true);
-    } else {  // l0.re*a.im - l0.im*a.re - l1.re*b.im + l1.im*b.re
-        set(0, l0.x, l0.y, a.z, a.w, false); set(1, l0.z, l0.w, a.x, a.y, true);
-        set(2, l1.x, l1.y, b.z, b.w, true); set(3, l1.z, l1.w, b.x, b.y, false);
-    }
-    return df_dot<4>(uh, ul, xh, xl);
-}
-
-// c * p + q2 * r in double-float: the rot_pair formulas with (c, s) = (ch + cl, sh + sl).
-__device__ __forceinline__ void df_lin2(float ch, float cl, float p_h, float p_l, float dh, float dl, float q_h,
-                                        float q_l, float& oh, float& ol) {
-    const float uh[2] = {ch, dh}, ul[2] = {cl, dl}, xh[2] = {p_h, q_h}, xl[2] = {p_l, q_l};
-    df_dot_pair<2>(uh, ul, xh, xl, oh, ol);
-}
-
-template <int AXIS>
-__device__ __forceinline__ void df_rot_pair(float ch, float cl, float sh, float sl, float4& a, float4& b) {
-    float4 na, nb;
-    if (AXIS == QS_GATE_RY) {  // [[c, -s], [s, c]]
-        df_lin2(ch, cl, a.x, a.y, -sh, -sl, b.x, b.y, na.x, na.y);
-        df_lin2(ch, cl, a.z, a.w, -sh, -sl, b.z, b.w, na.z, na.w);
-        df_lin2(sh, sl, a.x, a.y, ch, cl, b.x, b.y, nb.x, nb.y);
-        df_lin2(sh, sl, a.z, a.w, ch, cl, b.z, b.w, nb.z, nb.w);
-    } else if (AXIS == QS_GATE_RZ) {  // diag(c - i s, c + i s)
-        df_lin2(ch, cl, a.x, a.y, sh, sl, a.z, a.w, na.x, na.y);
-        df_lin2(ch, cl, a.z, a.w, -sh, -sl, a.x, a.y, na.z, na.w);
-        df_lin2(ch, cl, b.x, b.y, -sh, -sl, b.z, b.w, nb.x, nb.y);
-        df_lin2(ch, cl, b.z, b.w, sh, sl, b.x, b.y, nb.z, nb.w);
-    } else {  // RX: [[c, -i s], [-i s, c]]
-        df_lin2(ch, cl, a.x, a.y, sh, sl, b.z, b.w, na.x, na.y);
-        df_lin2(ch, cl, a.z, a.w, -sh, -sl, b.x, b.y, na.z, na.w);
-        df_lin2(ch, cl, b.x, b.y, sh, sl, a.z, a.w, nb.x, nb.y);
-        df_lin2(ch, cl, b.z, b.w, -sh, -sl, a.x, a.y, nb.z, nb.w);
-    }
-    a = na;
-    b = nb;
 }
 
 template <int AXIS>

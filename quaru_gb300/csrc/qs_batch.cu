@@ -1,18 +1,20 @@
 // qs_batch.cu — forward + adjoint gradients for a batch of circuits in one persistent launch.
 //
-// No counterpart in the reference. Work item = (circuit c, step s, chunk j):
-// steps 0..G-1 apply the circuit's gates, step G forms lambda = H psi and the
-// energy partial sums, steps G+1..2G walk the gates backwards (adjoint
-// rotations with per-chunk partial derivatives; fixed gates un-applied from
-// psi and lambda). Items are ordered by step round across circuits, so an item
-// only ever waits for items handed out before it; those are held by running
-// CTAs, which makes the schedule deadlock-free without any co-residency
-// assumption. Every wait is bounded: when it gives up it raises an error flag
-// that makes every CTA return, and the host reports QS_TIMEOUT.
+// No counterpart in the reference. Each circuit's gates are planned into tiled stages (the planner
+// of the fused forward path, qs_plan.cpp): forward stages, one step forming lambda = H psi with the
+// energy partial sums, and reverse stages walking the gates backwards (rotations with their
+// Im<lambda|A|psi> partials, fixed gates un-applied from psi and lambda). A work item is
+// (circuit c, step s, chunk j): a range of tiles of one stage, each tile loaded once into shared
+// memory, taken through all of the stage's gates and written back once (or, for the H psi step, a
+// range of amplitude pairs). Items are ordered by step round across circuits, so an item only ever
+// waits for items handed out before it; those are held by running CTAs, which makes the schedule
+// deadlock-free without any co-residency assumption. Every wait is bounded: when it gives up it
+// raises an error flag that makes every CTA return, and the host reports QS_TIMEOUT.
 //
-// The whole pass (parameter upload, state reset, persistent kernel, partial
-// reduction, result download) is captured once in a CUDA graph; a run writes
-// new parameters into pinned memory and replays it.
+// The whole pass (parameter upload, state reset, persistent kernel, partial reduction, result
+// download) is captured once in a CUDA graph; a run writes new parameters into pinned memory and
+// replays it. Complex128 batches with QS_ARITH_DF64 hold the tiles of stages made of rotations and
+// CNOTs as double-float values (FP32 pipe), with the inner products accumulated in FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,24 +31,44 @@
 #include "qs_device.cuh"
 #include "qs_kernels.h"
 #include "qs_reduce.cuh"
+#include "qs_rot.cuh"
+#include "qs_tile.h"
 
 namespace qs {
 namespace {
 
 constexpr int kBT = 256;
 constexpr int kFix1 = 16;  // fixed dense 1-qubit gate
-constexpr int kCnot = 17;  // CNOT (q0 = target, q1 = control)
+constexpr int kCnot = 17;  // CNOT
+constexpr int kBTileMax = 11;  // tile qubits
+constexpr int kBMaxRot = kMaxStageOps;  // rotations per stage
 constexpr long long kWaitCycles = 20000000000LL;  // ~10 s at 2 GHz: dependency waits give up after this
 
 struct BCirc {
     unsigned long long psi, lam;
-    int n, ngates, gate_off, nterms, term_off, nsteps, counter_off, part_off, nch_log, nrot;
+    int n, nterms, term_off, nsteps, counter_off, nrot;
+    int epart_off, rpart_off;  // partials: energy (2^nche_log), then rotation r at rpart_off + r * 2^ncht_log
+    int nche_log, ncht_log;    // chunks of the H psi step and of every tile stage
+    int T, stage_off, nfwd;    // tile qubits, first stage, forward stages (step nfwd is H psi)
 };
 
-struct BGate {
-    int kind, q0, q1, cs;
-    int rslot, pad0, pad1, pad2;
-    double m[8];  // kFix1: the 2x2 matrix; its adjoint is formed on the fly
+struct BStage {
+    int op_off, nops, nrot, df;  // df: double-float tiles
+    int L, H, pad0, pad1;
+    uint8_t pos[16];   // the tile's qubits, sorted (its base index skips them)
+    uint8_t high[8];   // qubit of local bit L + b
+};
+
+struct BOp {
+    int kind;   // QS_GATE_RX / RY / RZ, kFix1, kCnot
+    int tb;     // local target bit
+    int cb;     // CNOT: local control bit, or -1
+    int cglob;  // CNOT: control qubit outside the tile, or -1
+    int cs;     // rotation: index of (cos, sin) of theta/2
+    int rslot;  // rotation: circuit-level slot
+    int lrot;   // rotation: stage-local slot
+    int pad;
+    double m[8];  // kFix1: the 2x2 matrix (forward); its adjoint is formed on the fly
 };
 
 struct BPauli {
@@ -67,24 +89,10 @@ template <>
 struct St<float2> {
     static __device__ __forceinline__ float2 ld(const float2* p, uint64_t i) { return __ldcg(p + i); }
     static __device__ __forceinline__ void st(float2* p, uint64_t i, float2 v) { __stcg(p + i, v); }
-    static __device__ __forceinline__ double2 d(float2 v) { return make_double2(v.x, v.y); }
+    // integer-pipe conversion (exact for normal floats; subnormals read as zero)
+    static __device__ __forceinline__ double2 d(float2 v) { return make_double2(df_f2d(v.x), df_f2d(v.y)); }
     static __device__ __forceinline__ float2 from(double2 v) { return make_float2(float(v.x), float(v.y)); }
 };
-
-// R_A(theta) on a pair, with (c, s) = (cos, sin) of theta/2 (s negated for the inverse).
-template <typename R>
-__device__ __forceinline__ void rot(int kind, R c, R s, R& ax, R& ay, R& bx, R& by) {
-    if (kind == QS_GATE_RY) {
-        const R nax = c * ax - s * bx, nay = c * ay - s * by, nbx = s * ax + c * bx, nby = s * ay + c * by;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    } else if (kind == QS_GATE_RZ) {
-        const R nax = c * ax + s * ay, nay = c * ay - s * ax, nbx = c * bx - s * by, nby = c * by + s * bx;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    } else {
-        const R nax = c * ax + s * by, nay = c * ay - s * bx, nbx = c * bx + s * ay, nby = c * by - s * ax;
-        ax = nax; ay = nay; bx = nbx; by = nby;
-    }
-}
 
 // y = M x for a 2x2 complex matrix (adjoint: M^H).
 __device__ __forceinline__ void mat2(const double* m, bool adj, double2& a, double2& b) {
@@ -101,12 +109,6 @@ __device__ __forceinline__ void mat2(const double* m, bool adj, double2& a, doub
     b = make_double2(u[4] * x.x - u[5] * x.y + u[6] * y.x - u[7] * y.y, u[4] * x.y + u[5] * x.x + u[6] * y.y + u[7] * y.x);
 }
 
-__device__ __forceinline__ double im_lam_a_psi(int kind, double2 l0, double2 l1, double2 a, double2 b) {
-    if (kind == QS_GATE_RX) return (l0.x * b.y - l0.y * b.x) + (l1.x * a.y - l1.y * a.x);
-    if (kind == QS_GATE_RY) return (l1.x * a.x + l1.y * a.y) - (l0.x * b.x + l0.y * b.y);
-    return (l0.x * a.y - l0.y * a.x) - (l1.x * b.y - l1.y * b.x);
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kBT) k_batch_reset(const BCirc* __restrict__ circs) {
     const BCirc C = circs[blockIdx.y];
@@ -116,16 +118,101 @@ __global__ void __launch_bounds__(kBT) k_batch_reset(const BCirc* __restrict__ c
         St<T>::st(psi, i, St<T>::from(make_double2(i == 0 ? 1.0 : 0.0, 0.0)));
 }
 
+__device__ __forceinline__ uint32_t pair_index(uint32_t p, int tb) {
+    return ((p >> tb) << (tb + 1)) | (p & ((1u << tb) - 1u));
+}
+
+// One gate of a stage on the tile(s) in shared memory. fwd: psi only; reverse: psi and lambda, with
+// a rotation's inner-product term accumulated (before it is un-applied) into acc.
+template <typename T, int AXIS>
+__device__ __forceinline__ double tile_rot(T* sp, T* sl, uint32_t half, int tb, double c, double sn, bool fwd) {
+    using R = decltype(T().x);
+    const R cc = R(c), ss = R(fwd ? sn : -sn);
+    double acc = 0.0;
+    DfAcc facc;  // complex64: compensated FP32 products, rounded to FP64 once per thread
+    for (uint32_t p = threadIdx.x; p < half; p += kBT) {
+        const uint32_t i0 = pair_index(p, tb), i1 = i0 | (1u << tb);
+        T a = sp[i0], b = sp[i1];
+        if (!fwd) {
+            T l0 = sl[i0], l1 = sl[i1];
+            if constexpr (sizeof(R) == 8)
+                acc += im_term<AXIS>(l0, l1, a, b);
+            else
+                im_term_acc<AXIS>(facc, l0, l1, a, b);
+            rot_pair<AXIS>(cc, ss, l0.x, l0.y, l1.x, l1.y);
+            sl[i0] = l0;
+            sl[i1] = l1;
+        }
+        rot_pair<AXIS>(cc, ss, a.x, a.y, b.x, b.y);
+        sp[i0] = a;
+        sp[i1] = b;
+    }
+    if constexpr (sizeof(R) == 4) acc = __dadd_rn(df_f2d(facc.s), df_f2d(facc.c));
+    return acc;
+}
+
+template <int AXIS>
+__device__ __forceinline__ double tile_rot_df(float4* sp, float4* sl, uint32_t half, int tb, double c, double sn,
+                                              bool fwd) {
+    float ch, cl, sh, slo;
+    df_split(c, ch, cl);
+    df_split(fwd ? sn : -sn, sh, slo);
+    double acc = 0.0;
+    for (uint32_t p = threadIdx.x; p < half; p += kBT) {
+        const uint32_t i0 = pair_index(p, tb), i1 = i0 | (1u << tb);
+        float4 a = sp[i0], b = sp[i1];
+        if (!fwd) {
+            float4 l0 = sl[i0], l1 = sl[i1];
+            acc += adj_im_df<AXIS>(l0, l1, a, b);
+            df_rot_pair<AXIS>(ch, cl, sh, slo, l0, l1);
+            sl[i0] = l0;
+            sl[i1] = l1;
+        }
+        df_rot_pair<AXIS>(ch, cl, sh, slo, a, b);
+        sp[i0] = a;
+        sp[i1] = b;
+    }
+    return acc;
+}
+
+template <typename E>
+__device__ __forceinline__ void tile_cnot(E* s, uint32_t half, int tb, int cb) {
+    for (uint32_t p = threadIdx.x; p < half; p += kBT) {
+        const uint32_t i0 = pair_index(p, tb);
+        if (cb >= 0 && !((i0 >> cb) & 1u)) continue;
+        const uint32_t i1 = i0 | (1u << tb);
+        const E t = s[i0];
+        s[i0] = s[i1];
+        s[i1] = t;
+    }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, const BGate* __restrict__ gates,
-                                               const BPauli* __restrict__ terms, const double2* __restrict__ cs,
-                                               const uint32_t* __restrict__ seg_first, const int4* __restrict__ segs,
-                                               int nsegs, uint32_t nitems, int chunk_log,
+__device__ __forceinline__ void tile_fix1(T* s, uint32_t half, int tb, const double* m, bool adj) {
+    for (uint32_t p = threadIdx.x; p < half; p += kBT) {
+        const uint32_t i0 = pair_index(p, tb), i1 = i0 | (1u << tb);
+        double2 a = St<T>::d(s[i0]), b = St<T>::d(s[i1]);
+        mat2(m, adj, a, b);
+        s[i0] = St<T>::from(a);
+        s[i1] = St<T>::from(b);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, const BStage* __restrict__ stages,
+                                               const BOp* __restrict__ ops, const BPauli* __restrict__ terms,
+                                               const double2* __restrict__ cs, const uint32_t* __restrict__ seg_first,
+                                               const int4* __restrict__ segs, int nsegs, uint32_t nitems,
                                                unsigned int* __restrict__ counters, double* __restrict__ partials,
                                                unsigned int* __restrict__ ticket, int* __restrict__ err) {
-    using R = decltype(T().x);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sp = reinterpret_cast<T*>(smem_raw);
+    T* sl = sp + (1u << kBTileMax);
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sl + (1u << kBTileMax));
+    double* sacc = reinterpret_cast<double*>(rowoff + 64);  // [kBMaxRot][8 warps]
     __shared__ uint32_t s_item;
     __shared__ int s_seg, s_stop;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (;;) {
         if (threadIdx.x == 0) {
             s_item = atomicAdd(ticket, 1u);
@@ -142,13 +229,13 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
         __syncthreads();
         if (s_stop) return;
         const int4 sg = segs[s_seg];
-        const int c = sg.x, s = sg.y, nch = sg.z;
+        const int c = sg.x, s = sg.y, prevnch = sg.w;
         const uint32_t j = s_item - seg_first[s_seg];
         const BCirc C = circs[c];
         if (s > 0 && threadIdx.x == 0) {  // every chunk of the previous step must be done
             volatile unsigned int* prev = counters + C.counter_off + s - 1;
             const long long t0 = clock64();
-            while (*prev < unsigned(nch)) {
+            while (*prev < unsigned(prevnch)) {
                 __nanosleep(100);
                 if (clock64() - t0 > kWaitCycles) {
                     atomicExch(err, 1);
@@ -162,65 +249,9 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
         if (s_stop) return;
         T* psi = reinterpret_cast<T*>(C.psi);
         T* lam = reinterpret_cast<T*>(C.lam);
-        const int G = C.ngates;
-        const int cl = min(chunk_log, C.n - 1);
-        const uint64_t pairs = 1ull << (C.n - 1);
-        const uint64_t p0 = uint64_t(j) << cl;
-        const uint64_t p1 = (p0 + (1ull << cl) < pairs) ? p0 + (1ull << cl) : pairs;
-        if (s < G || s > G) {
-            const bool fwd = s < G;
-            const BGate g = gates[C.gate_off + (fwd ? s : 2 * G - s)];
-            const uint64_t lo = (1ull << g.q0) - 1ull, tb = 1ull << g.q0;
-            R cc = 0, ss = 0;
-            if (g.kind <= QS_GATE_RZ) {
-                const double2 t = cs[g.cs];
-                cc = R(t.x);
-                ss = R(fwd ? t.y : -t.y);
-            }
-            double acc = 0.0;
-            for (uint64_t p = p0 + threadIdx.x; p < p1; p += kBT) {
-                const uint64_t i0 = ((p & ~lo) << 1) | (p & lo), i1 = i0 | tb;
-                if (g.kind == kCnot) {
-                    if (!((i0 >> g.q1) & 1ull)) continue;
-                    const T a = St<T>::ld(psi, i0), b = St<T>::ld(psi, i1);
-                    St<T>::st(psi, i0, b);
-                    St<T>::st(psi, i1, a);
-                    if (!fwd) {
-                        const T la = St<T>::ld(lam, i0), lb = St<T>::ld(lam, i1);
-                        St<T>::st(lam, i0, lb);
-                        St<T>::st(lam, i1, la);
-                    }
-                } else if (g.kind == kFix1) {
-                    double2 a = St<T>::d(St<T>::ld(psi, i0)), b = St<T>::d(St<T>::ld(psi, i1));
-                    mat2(g.m, !fwd, a, b);
-                    St<T>::st(psi, i0, St<T>::from(a));
-                    St<T>::st(psi, i1, St<T>::from(b));
-                    if (!fwd) {
-                        double2 la = St<T>::d(St<T>::ld(lam, i0)), lb = St<T>::d(St<T>::ld(lam, i1));
-                        mat2(g.m, true, la, lb);
-                        St<T>::st(lam, i0, St<T>::from(la));
-                        St<T>::st(lam, i1, St<T>::from(lb));
-                    }
-                } else {
-                    T a = St<T>::ld(psi, i0), b = St<T>::ld(psi, i1);
-                    if (!fwd) {
-                        T l0 = St<T>::ld(lam, i0), l1 = St<T>::ld(lam, i1);
-                        acc += im_lam_a_psi(g.kind, St<T>::d(l0), St<T>::d(l1), St<T>::d(a), St<T>::d(b));
-                        rot<R>(g.kind, cc, ss, l0.x, l0.y, l1.x, l1.y);
-                        St<T>::st(lam, i0, l0);
-                        St<T>::st(lam, i1, l1);
-                    }
-                    rot<R>(g.kind, cc, ss, a.x, a.y, b.x, b.y);
-                    St<T>::st(psi, i0, a);
-                    St<T>::st(psi, i1, b);
-                }
-            }
-            if (!fwd && g.kind <= QS_GATE_RZ) {
-                double dummy = 0.0;
-                rd_block_sum2<kBT>(acc, dummy);
-                if (threadIdx.x == 0) partials[C.part_off + (1 + g.rslot) * nch + j] = acc;
-            }
-        } else {  // lambda = H psi over amplitudes [2 p0, 2 p1), energy partial
+        if (s == C.nfwd) {  // lambda = H psi over amplitudes [2 p0, 2 p1), energy partial
+            const int cl = C.n - 1 - C.nche_log;
+            const uint64_t p0 = uint64_t(j) << cl, p1 = p0 + (1ull << cl);
             double e = 0.0;
             for (uint64_t i = 2 * p0 + threadIdx.x; i < 2 * p1; i += kBT) {
                 double re = 0.0, im = 0.0;
@@ -238,12 +269,122 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
                     }
                 }
                 St<T>::st(lam, i, St<T>::from(make_double2(re, im)));
-                const double2 p = St<T>::d(St<T>::ld(psi, i));
-                e = fma(p.x, re, fma(p.y, im, e));
+                const double2 pv = St<T>::d(St<T>::ld(psi, i));
+                e = fma(pv.x, re, fma(pv.y, im, e));
             }
             double dummy = 0.0;
             rd_block_sum2<kBT>(e, dummy);
-            if (threadIdx.x == 0) partials[C.part_off + j] = e;
+            if (threadIdx.x == 0) partials[C.epart_off + j] = e;
+        } else {  // a tiled stage: tiles [j * tpi, (j + 1) * tpi)
+            const bool fwd = s < C.nfwd;
+            const BStage S = stages[C.stage_off + (fwd ? s : s - 1)];
+            const uint32_t tsize = 1u << C.T, half = tsize >> 1;
+            const uint64_t tpi = 1ull << (C.n - C.T - C.ncht_log);
+            const uint32_t lmask = (1u << S.L) - 1u;
+            for (int r = threadIdx.x; r < (1 << S.H); r += kBT) {
+                uint64_t o = 0;
+                for (int b = 0; b < S.H; b++)
+                    if (r >> b & 1) o |= 1ull << S.high[b];
+                rowoff[r] = o;
+            }
+            if (!fwd)
+                for (int r = threadIdx.x; r < S.nrot * (kBT / 32); r += kBT) sacc[r] = 0.0;
+            __syncthreads();
+            float4* fp = reinterpret_cast<float4*>(sp);
+            float4* fl = reinterpret_cast<float4*>(sl);
+            const bool df = sizeof(T) == 16 && S.df;
+            for (uint64_t t = uint64_t(j) * tpi; t < uint64_t(j + 1) * tpi; t++) {
+                uint64_t base = t;  // insert the tile's qubits as zero bits
+                for (int k = 0; k < C.T; k++) {
+                    const int q = S.pos[k];
+                    base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
+                }
+                for (uint32_t i = threadIdx.x; i < tsize; i += kBT) {
+                    const uint64_t g = base + rowoff[i >> S.L] + (i & lmask);
+                    const T v = St<T>::ld(psi, g);
+                    T w = v;
+                    if (!fwd) w = St<T>::ld(lam, g);
+                    if (df) {
+                        const double2 dv = St<T>::d(v), dw = St<T>::d(w);
+                        float4 f;
+                        df_split(dv.x, f.x, f.y);
+                        df_split(dv.y, f.z, f.w);
+                        fp[i] = f;
+                        if (!fwd) {
+                            df_split(dw.x, f.x, f.y);
+                            df_split(dw.y, f.z, f.w);
+                            fl[i] = f;
+                        }
+                    } else {
+                        sp[i] = v;
+                        if (!fwd) sl[i] = w;
+                    }
+                }
+                __syncthreads();
+                for (int o = 0; o < S.nops; o++) {
+                    const BOp op = ops[S.op_off + o];
+                    if (op.kind == kCnot) {
+                        if (op.cglob < 0 || ((base >> op.cglob) & 1ull)) {  // outside control: the whole tile
+                            if (df) {
+                                tile_cnot(fp, half, op.tb, op.cb);
+                                if (!fwd) tile_cnot(fl, half, op.tb, op.cb);
+                            } else {
+                                tile_cnot(sp, half, op.tb, op.cb);
+                                if (!fwd) tile_cnot(sl, half, op.tb, op.cb);
+                            }
+                        }
+                    } else if (op.kind == kFix1) {  // never in double-float stages
+                        if constexpr (true) {
+                            tile_fix1(sp, half, op.tb, op.m, !fwd);
+                            if (!fwd) tile_fix1(sl, half, op.tb, op.m, true);
+                        }
+                    } else {
+                        const double2 t2 = cs[op.cs];
+                        double v;
+                        if (df) {
+                            if (op.kind == QS_GATE_RX) v = tile_rot_df<QS_GATE_RX>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            else if (op.kind == QS_GATE_RY) v = tile_rot_df<QS_GATE_RY>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            else v = tile_rot_df<QS_GATE_RZ>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                        } else {
+                            if (op.kind == QS_GATE_RX) v = tile_rot<T, QS_GATE_RX>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                            else if (op.kind == QS_GATE_RY) v = tile_rot<T, QS_GATE_RY>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                            else v = tile_rot<T, QS_GATE_RZ>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                        }
+                        if (!fwd) {
+#pragma unroll
+                            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+                            if (lane == 0) sacc[op.lrot * (kBT / 32) + warp] += v;
+                        }
+                    }
+                    __syncthreads();
+                }
+                for (uint32_t i = threadIdx.x; i < tsize; i += kBT) {
+                    const uint64_t g = base + rowoff[i >> S.L] + (i & lmask);
+                    if (df) {
+                        const float4 f = fp[i];
+                        St<T>::st(psi, g, St<T>::from(make_double2(__dadd_rn(df_f2d(f.x), df_f2d(f.y)),
+                                                                   __dadd_rn(df_f2d(f.z), df_f2d(f.w)))));
+                        if (!fwd) {
+                            const float4 h = fl[i];
+                            St<T>::st(lam, g, St<T>::from(make_double2(__dadd_rn(df_f2d(h.x), df_f2d(h.y)),
+                                                                       __dadd_rn(df_f2d(h.z), df_f2d(h.w)))));
+                        }
+                    } else {
+                        St<T>::st(psi, g, sp[i]);
+                        if (!fwd) St<T>::st(lam, g, sl[i]);
+                    }
+                }
+                __syncthreads();
+            }
+            if (!fwd) {  // this item's partial of every rotation of the stage
+                for (int o = threadIdx.x; o < S.nops; o += kBT) {
+                    const BOp op = ops[S.op_off + o];
+                    if (op.kind == kCnot || op.kind == kFix1) continue;
+                    double v = 0.0;
+                    for (int w = 0; w < kBT / 32; w++) v += sacc[op.lrot * (kBT / 32) + w];
+                    partials[C.rpart_off + size_t(op.rslot << C.ncht_log) + j] = v;
+                }
+            }
         }
         __threadfence();
         __syncthreads();
@@ -267,12 +408,12 @@ __global__ void __launch_bounds__(kBT) k_batch_reduce(const double* __restrict__
 }  // namespace qs
 
 struct qs_batch {
-    int prec = QS_PREC_C128, count = 0, sms = 1, chunk_log = 12, ctas = 2;
+    int prec = QS_PREC_C128, arith = QS_ARITH_FMA, count = 0, sms = 1, chunk_log = 12, ctas = 2;
     cudaStream_t stream = nullptr;
     unsigned char* arena = nullptr;
-    size_t arena_bytes = 0;
     qs::BCirc* dcirc = nullptr;
-    qs::BGate* dgates = nullptr;
+    qs::BStage* dstages = nullptr;
+    qs::BOp* dops = nullptr;
     qs::BPauli* dterms = nullptr;
     double2* dcs = nullptr;
     uint32_t* dseg_first = nullptr;
@@ -288,7 +429,7 @@ struct qs_batch {
     int* herr = nullptr;      // pinned
     int nsegs = 0, nres = 0, ncs = 0, ncounters = 0;
     uint32_t nitems = 0;
-    size_t total_params = 0;
+    size_t total_params = 0, smem = 0;
     std::vector<size_t> param_off;
     std::vector<int> cs_param;       // parameter index (global) of each rotation
     std::vector<int> res_circ_base;  // first result of each circuit
@@ -301,8 +442,6 @@ struct qs_batch {
 namespace {
 
 using namespace qs;
-
-thread_local std::string g_batch_err;
 
 bool is_cnot(const qs_param_gate& g) {
     if (g.k != 2 || !g.matrix) return false;
@@ -328,9 +467,11 @@ void release(qs_batch* b) {
     delete b;
 }
 
-// Work-item schedule for a chunk size: segments (circuit, step, chunks) ordered by step round.
-void build_schedule(qs_batch* b, int chunk_log, std::vector<uint32_t>* first, std::vector<int4>* segs,
-                    uint64_t* nitems) {
+// Chunks of step s of circuit C for the current chunk size (the H psi step counts pair chunks).
+int step_chunks(const BCirc& C, int s) { return 1 << (s == C.nfwd ? C.nche_log : C.ncht_log); }
+
+// Work-item schedule: segments (circuit, step, chunks, chunks of the previous step) by step round.
+void build_schedule(qs_batch* b, std::vector<uint32_t>* first, std::vector<int4>* segs, uint64_t* nitems) {
     first->clear();
     segs->clear();
     int maxsteps = 0;
@@ -340,13 +481,17 @@ void build_schedule(qs_batch* b, int chunk_log, std::vector<uint32_t>* first, st
         for (int c = 0; c < b->count; c++) {
             const BCirc& C = b->hcirc[c];
             if (s >= C.nsteps) continue;
-            const int cl = std::min(chunk_log, C.n - 1);
-            const int nch = 1 << (C.n - 1 - cl);
+            const int nch = step_chunks(C, s);
             first->push_back(uint32_t(item));
-            segs->push_back(make_int4(c, s, nch, 0));
+            segs->push_back(make_int4(c, s, nch, s > 0 ? step_chunks(C, s - 1) : 0));
             item += uint64_t(nch);
         }
     *nitems = item;
+}
+
+size_t batch_smem(int prec) {
+    const size_t amp = prec == QS_PREC_C64 ? 8 : 16;
+    return 2 * (amp << kBTileMax) + 64 * 8 + size_t(kBMaxRot) * (kBT / 32) * 8;
 }
 
 cudaError_t capture(qs_batch* b) {
@@ -362,14 +507,14 @@ cudaError_t capture(qs_batch* b) {
     const dim3 rg(uint32_t(b->sms * 2), uint32_t(b->count));
     if (b->prec == QS_PREC_C64) {
         k_batch_reset<float2><<<rg, kBT, 0, s>>>(b->dcirc);
-        k_batch<float2><<<b->sms * b->ctas, kBT, 0, s>>>(b->dcirc, b->dgates, b->dterms, b->dcs, b->dseg_first,
-                                                         b->dsegs, b->nsegs, b->nitems, b->chunk_log, b->dcounters,
-                                                         b->dpart, b->dticket, b->derr);
+        k_batch<float2><<<b->sms * b->ctas, kBT, b->smem, s>>>(b->dcirc, b->dstages, b->dops, b->dterms, b->dcs,
+                                                               b->dseg_first, b->dsegs, b->nsegs, b->nitems,
+                                                               b->dcounters, b->dpart, b->dticket, b->derr);
     } else {
         k_batch_reset<double2><<<rg, kBT, 0, s>>>(b->dcirc);
-        k_batch<double2><<<b->sms * b->ctas, kBT, 0, s>>>(b->dcirc, b->dgates, b->dterms, b->dcs, b->dseg_first,
-                                                          b->dsegs, b->nsegs, b->nitems, b->chunk_log, b->dcounters,
-                                                          b->dpart, b->dticket, b->derr);
+        k_batch<double2><<<b->sms * b->ctas, kBT, b->smem, s>>>(b->dcirc, b->dstages, b->dops, b->dterms, b->dcs,
+                                                                b->dseg_first, b->dsegs, b->nsegs, b->nitems,
+                                                                b->dcounters, b->dpart, b->dticket, b->derr);
     }
     k_batch_reduce<<<std::min(b->nres, b->sms * 8), kBT, 0, s>>>(b->dpart, b->drtab, b->nres, b->dres);
     cudaMemcpyAsync(b->hres, b->dres, sizeof(double) * b->nres, cudaMemcpyDeviceToHost, s);
@@ -377,20 +522,6 @@ cudaError_t capture(qs_batch* b) {
     e = cudaStreamEndCapture(s, &b->graph);
     if (e != cudaSuccess) return e;
     return cudaGraphInstantiate(&b->exec, b->graph, 0);
-}
-
-// Upload a schedule for chunk_log into the arena's schedule area (sized for the smallest chunk).
-cudaError_t upload_schedule(qs_batch* b, int chunk_log) {
-    std::vector<uint32_t> first;
-    std::vector<int4> segs;
-    uint64_t n = 0;
-    build_schedule(b, chunk_log, &first, &segs, &n);
-    b->nsegs = int(segs.size());
-    b->nitems = uint32_t(n);
-    b->chunk_log = chunk_log;
-    cudaError_t e = cudaMemcpy(b->dseg_first, first.data(), first.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(b->dsegs, segs.data(), segs.size() * sizeof(int4), cudaMemcpyHostToDevice);
-    return e;
 }
 
 std::string cache_path() {
@@ -421,6 +552,94 @@ void cache_store(const std::string& key, int cl, int ct) {
     if (f) f << key << " " << cl << " " << ct << "\n";
 }
 
+// Planning form of one gate (targets forced into the tile, controls free): rotations and fixed
+// 1-qubit gates as dense 1-qubit gates on their target, CNOT as classified (target + control).
+OpDesc plan_desc(const qs_param_gate& G, bool cnot) {
+    OpDesc d;
+    if (cnot) {
+        classify_gate(G.matrix, 2, G.targets, &d);
+        return d;
+    }
+    d.kind = OP_DENSE;
+    d.k = d.orig_k = 1;
+    d.tq[0] = int(G.targets[0]);
+    d.m.assign(8, 0.0);
+    d.touched_rows = 2;
+    return d;
+}
+
+// Stages of one circuit (forward gates, then the reverse sweep) into the stage and op tables.
+void plan_circuit(const qs_batch_circuit& q, int T, bool df_ok, BCirc* C, const std::vector<int>& cs_of,
+                  const std::vector<int>& rslot_of, std::vector<BStage>* stages, std::vector<BOp>* ops) {
+    const int n = int(q.n), L = std::min(5, T);
+    std::vector<char> cnot(q.m);
+    std::vector<OpDesc> fw;
+    for (size_t g = 0; g < q.m; g++) {
+        cnot[g] = q.gates[g].kind == QS_GATE_FIXED && q.gates[g].k == 2;
+        fw.push_back(plan_desc(q.gates[g], cnot[g]));
+    }
+    auto emit = [&](const std::vector<int>& order, bool fwd) {
+        std::vector<OpDesc> list;
+        for (int g : order) list.push_back(fw[g]);
+        const std::vector<TileStage> st = plan_tiles(list, n, T, L, false);
+        int count = 0;
+        for (const TileStage& S : st) {
+            BStage B{};
+            B.op_off = int(ops->size());
+            B.L = S.L;
+            B.H = int(S.high.size());
+            std::vector<int> qpos;
+            for (int qb = 0; qb < S.L; qb++) qpos.push_back(qb);
+            for (int qb : S.high) qpos.push_back(qb);
+            std::sort(qpos.begin(), qpos.end());
+            for (size_t i = 0; i < qpos.size(); i++) B.pos[i] = uint8_t(qpos[i]);
+            for (int i = 0; i < B.H; i++) B.high[i] = uint8_t(S.high[i]);
+            auto local = [&](int qb) -> int {
+                if (qb < S.L) return qb;
+                for (int i = 0; i < B.H; i++)
+                    if (S.high[i] == qb) return S.L + i;
+                return -1;
+            };
+            B.df = df_ok ? 1 : 0;
+            for (int idx : S.ops) {
+                const int g = order[idx];
+                const qs_param_gate& G = q.gates[g];
+                BOp o{};
+                o.cb = o.cglob = -1;
+                if (cnot[g]) {  // CNOT's matrix: targets[1] = 1 swaps the rows of targets[0]
+                    o.kind = kCnot;
+                    o.tb = local(int(G.targets[0]));
+                    o.cb = local(int(G.targets[1]));
+                    if (o.cb < 0) o.cglob = int(G.targets[1]);
+                } else if (G.kind == QS_GATE_FIXED) {
+                    o.kind = kFix1;
+                    o.tb = local(int(G.targets[0]));
+                    for (int i = 0; i < 8; i++) o.m[i] = G.matrix[i];
+                    B.df = 0;  // double-float stages take rotations and CNOTs
+                } else {
+                    o.kind = G.kind;
+                    o.tb = local(int(G.targets[0]));
+                    o.cs = cs_of[g];
+                    o.rslot = rslot_of[g];
+                    o.lrot = B.nrot++;
+                }
+                ops->push_back(o);
+                B.nops++;
+            }
+            stages->push_back(B);
+            count++;
+        }
+        return count;
+    };
+    std::vector<int> order(q.m);
+    for (size_t g = 0; g < q.m; g++) order[g] = int(g);
+    C->stage_off = int(stages->size());
+    C->nfwd = emit(order, true);
+    std::reverse(order.begin(), order.end());
+    const int nrev = emit(order, false);
+    C->nsteps = C->nfwd + 1 + nrev;
+}
+
 }  // namespace
 
 extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, const qs_batch_options* opts,
@@ -433,20 +652,23 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
     *out = nullptr;
     qs_batch_options o{};
     o.precision = QS_PREC_C128;
+    o.arith = QS_ARITH_FMA;
     if (opts) o = *opts;
     if (o.precision != QS_PREC_C128 && o.precision != QS_PREC_C64) return fail(QS_INVALID_ARGUMENT, "unknown precision");
     auto* b = new qs_batch();
     b->prec = o.precision;
+    b->arith = o.arith;
     b->count = int(count);
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
-    // ---- validate and build host tables
-    std::vector<BGate> gates;
+    // ---- validate and plan
+    std::vector<BStage> stages;
+    std::vector<BOp> ops;
     std::vector<BPauli> terms;
-    std::vector<int2> rtab;
-    size_t amp = b->prec == QS_PREC_C64 ? 8 : 16, state_bytes = 0;
-    int counters = 0, minlog = 30;
+    const size_t amp = b->prec == QS_PREC_C64 ? 8 : 16;
+    size_t state_bytes = 0;
+    int counters = 0;
     for (size_t c = 0; c < count; c++) {
         const qs_batch_circuit& q = circuits[c];
         if (q.n < 1 || q.n > 30 || (q.m && !q.gates) || (q.nterms && !q.terms)) {
@@ -456,19 +678,14 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
         }
         BCirc C{};
         C.n = int(q.n);
-        C.ngates = int(q.m);
-        C.gate_off = int(gates.size());
+        C.T = std::min(kBTileMax, C.n);
         C.nterms = int(q.nterms);
         C.term_off = int(terms.size());
-        C.nsteps = 2 * int(q.m) + 1;
-        C.counter_off = counters;
-        counters += C.nsteps;
         b->param_off.push_back(b->total_params);
         b->total_params += q.nparams;
-        std::vector<int> rp;
+        std::vector<int> rp, cs_of(q.m, -1), rslot_of(q.m, -1);
         for (size_t g = 0; g < q.m; g++) {
             const qs_param_gate& G = q.gates[g];
-            BGate d{};
             const bool rotk = G.kind == QS_GATE_RX || G.kind == QS_GATE_RY || G.kind == QS_GATE_RZ;
             if (rotk) {
                 if (G.k != 1 || !G.targets || G.targets[0] >= q.n || G.param < 0 || size_t(G.param) >= q.nparams) {
@@ -477,28 +694,19 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
                     return fail(QS_INVALID_ARGUMENT, "circuit " + std::to_string(c) + " gate " + std::to_string(g) +
                                                          ": bad rotation");
                 }
-                d.kind = G.kind;
-                d.q0 = int(G.targets[0]);
-                d.cs = int(b->cs_param.size());
-                d.rslot = int(rp.size());
+                cs_of[g] = int(b->cs_param.size());
+                rslot_of[g] = int(rp.size());
                 b->cs_param.push_back(int(b->param_off[c]) + G.param);
                 rp.push_back(G.param);
             } else if (G.kind == QS_GATE_FIXED && G.k == 1 && G.matrix && G.targets && G.targets[0] < q.n) {
-                d.kind = kFix1;
-                d.q0 = int(G.targets[0]);
-                for (int i = 0; i < 8; i++) d.m[i] = G.matrix[i];
             } else if (G.kind == QS_GATE_FIXED && is_cnot(G) && G.targets && G.targets[0] < q.n &&
                        G.targets[1] < q.n && G.targets[0] != G.targets[1]) {
-                d.kind = kCnot;
-                d.q0 = int(G.targets[0]);
-                d.q1 = int(G.targets[1]);
             } else {
                 if (err) err[2] = c;
                 release(b);
                 return fail(QS_INVALID_ARGUMENT, "circuit " + std::to_string(c) + " gate " + std::to_string(g) +
                                                      ": the batch path takes rotations, 1-qubit gates and CNOTs");
             }
-            gates.push_back(d);
         }
         for (size_t t = 0; t < q.nterms; t++) {
             if ((q.terms[t].x_mask | q.terms[t].z_mask) >> q.n) {
@@ -509,31 +717,33 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
             terms.push_back({q.terms[t].coeff, q.terms[t].x_mask, q.terms[t].z_mask});
         }
         C.nrot = int(rp.size());
+        plan_circuit(q, C.T, b->prec == QS_PREC_C128 && b->arith == QS_ARITH_DF64, &C, cs_of, rslot_of, &stages,
+                     &ops);
+        C.counter_off = counters;
+        counters += C.nsteps;
         b->rot_param.push_back(rp);
         state_bytes += 2 * al((size_t(1) << q.n) * amp);
-        minlog = std::min(minlog, C.n - 1);
         b->hcirc.push_back(C);
     }
     b->ncs = int(b->cs_param.size());
     b->ncounters = counters;
-    // partial and result tables depend on the chunk size; size them for the smallest candidate (2^8 pairs)
+    // partial tables depend on the chunk size; size them for the smallest candidate (2^8 pairs per item)
     const int kMinChunk = 8;
-    size_t part_max = 0;
+    size_t part_max = 0, max_segs = 0;
     for (const BCirc& C : b->hcirc) {
-        const int nch = 1 << (C.n - 1 - std::min(kMinChunk, C.n - 1));
-        part_max += size_t(1 + C.nrot) * nch;
+        part_max += (size_t(1) << (C.n - 1 - std::min(kMinChunk, C.n - 1))) + size_t(C.nrot) * (size_t(1) << (C.n - C.T));
+        max_segs += size_t(C.nsteps);
     }
+    std::vector<int2> rtab;
     for (int c = 0; c < b->count; c++) {
         b->res_circ_base.push_back(int(rtab.size()));
         for (int r = 0; r <= b->hcirc[c].nrot; r++) rtab.push_back(make_int2(0, 0));
     }
     b->nres = int(rtab.size());
-    // segments: at most count * maxsteps
-    size_t max_segs = 0;
-    for (const BCirc& C : b->hcirc) max_segs += size_t(C.nsteps);
     // ---- arena
-    const size_t o_circ = 0, o_gates = o_circ + al(sizeof(BCirc) * count + 1),
-                 o_terms = o_gates + al(sizeof(BGate) * gates.size() + 1),
+    const size_t o_circ = 0, o_stages = o_circ + al(sizeof(BCirc) * count + 1),
+                 o_ops = o_stages + al(sizeof(BStage) * stages.size() + 1),
+                 o_terms = o_ops + al(sizeof(BOp) * ops.size() + 1),
                  o_cs = o_terms + al(sizeof(BPauli) * terms.size() + 1), o_first = o_cs + al(16 * (size_t(b->ncs) + 1)),
                  o_segs = o_first + al(4 * max_segs + 4), o_ctr = o_segs + al(sizeof(int4) * max_segs + 16),
                  o_part = o_ctr + al(4 * size_t(counters) + 4), o_res = o_part + al(8 * part_max + 8),
@@ -544,6 +754,11 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
     if (e == cudaSuccess) e = cudaMallocHost(&b->hcs, 16 * (size_t(b->ncs) + 1));
     if (e == cudaSuccess) e = cudaMallocHost(&b->hres, 8 * (size_t(b->nres) + 1));
     if (e == cudaSuccess) e = cudaMallocHost(&b->herr, sizeof(int));
+    b->smem = batch_smem(b->prec);
+    if (e == cudaSuccess)
+        e = b->prec == QS_PREC_C64
+                ? cudaFuncSetAttribute(k_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(b->smem))
+                : cudaFuncSetAttribute(k_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(b->smem));
     if (e != cudaSuccess) {
         release(b);
         return fail(e == cudaErrorMemoryAllocation ? QS_OUT_OF_MEMORY : QS_CUDA_ERROR,
@@ -551,7 +766,8 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
     }
     unsigned char* A = b->arena;
     b->dcirc = reinterpret_cast<BCirc*>(A + o_circ);
-    b->dgates = reinterpret_cast<BGate*>(A + o_gates);
+    b->dstages = reinterpret_cast<BStage*>(A + o_stages);
+    b->dops = reinterpret_cast<BOp*>(A + o_ops);
     b->dterms = reinterpret_cast<BPauli*>(A + o_terms);
     b->dcs = reinterpret_cast<double2*>(A + o_cs);
     b->dseg_first = reinterpret_cast<uint32_t*>(A + o_first);
@@ -569,33 +785,55 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
         C.lam = reinterpret_cast<unsigned long long>(A + off);
         off += al((size_t(1) << C.n) * amp);
     }
-    // per chunk size: partial offsets and result table
+    // per chunk size (2^cl amplitude pairs per item): chunk counts, partial offsets, result table,
+    // schedule
     auto layout = [&](int cl) {
         int part = 0;
         std::vector<int2> rt;
         for (auto& C : b->hcirc) {
-            const int nch = 1 << (C.n - 1 - std::min(cl, C.n - 1));
-            C.part_off = part;
-            C.nch_log = C.n - 1 - std::min(cl, C.n - 1);
-            for (int r = 0; r <= C.nrot; r++) rt.push_back(make_int2(part + r * nch, nch));
-            part += (1 + C.nrot) * nch;
+            C.nche_log = C.n - 1 - std::min(cl, C.n - 1);
+            C.ncht_log = (C.n - C.T) - std::min(C.n - C.T, std::max(0, cl + 1 - C.T));
+            C.epart_off = part;
+            part += 1 << C.nche_log;
+            C.rpart_off = part;
+            rt.push_back(make_int2(C.epart_off, 1 << C.nche_log));
+            for (int r = 0; r < C.nrot; r++) rt.push_back(make_int2(C.rpart_off + (r << C.ncht_log), 1 << C.ncht_log));
+            part += C.nrot << C.ncht_log;
         }
+        std::vector<uint32_t> first;
+        std::vector<int4> segs;
+        uint64_t n = 0;
+        build_schedule(b, &first, &segs, &n);
+        b->nsegs = int(segs.size());
+        b->nitems = uint32_t(n);
+        b->chunk_log = cl;
         cudaError_t e2 = cudaMemcpy(b->dcirc, b->hcirc.data(), sizeof(BCirc) * count, cudaMemcpyHostToDevice);
         if (e2 == cudaSuccess && !rt.empty())
             e2 = cudaMemcpy(b->drtab, rt.data(), sizeof(int2) * rt.size(), cudaMemcpyHostToDevice);
-        if (e2 == cudaSuccess) e2 = upload_schedule(b, cl);
+        if (e2 == cudaSuccess) e2 = cudaMemcpy(b->dseg_first, first.data(), first.size() * 4, cudaMemcpyHostToDevice);
+        if (e2 == cudaSuccess)
+            e2 = cudaMemcpy(b->dsegs, segs.data(), segs.size() * sizeof(int4), cudaMemcpyHostToDevice);
         return e2;
     };
-    if (!gates.empty()) e = cudaMemcpy(b->dgates, gates.data(), sizeof(BGate) * gates.size(), cudaMemcpyHostToDevice);
+    if (!stages.empty())
+        e = cudaMemcpy(b->dstages, stages.data(), sizeof(BStage) * stages.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !ops.empty())
+        e = cudaMemcpy(b->dops, ops.data(), sizeof(BOp) * ops.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !terms.empty())
         e = cudaMemcpy(b->dterms, terms.data(), sizeof(BPauli) * terms.size(), cudaMemcpyHostToDevice);
     for (int i = 0; i < b->ncs; i++) b->hcs[i] = make_double2(1.0, 0.0);
     // ---- chunk size and persistence: from options, the autotune cache, or by timing candidates
+    int max_per_sm = 1;
+    if (e == cudaSuccess)
+        e = b->prec == QS_PREC_C64
+                ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_batch<float2>, kBT, b->smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, k_batch<double2>, kBT, b->smem);
+    max_per_sm = std::max(1, max_per_sm);
     std::ostringstream key;
-    key << "batch:p" << b->prec << ":c" << count << ":items";
+    key << "batch2:p" << b->prec << ":a" << (b->arith == QS_ARITH_DF64) << ":c" << count << ":items";
     {
         uint64_t sig = 0;
-        for (const BCirc& C : b->hcirc) sig = sig * 1315423911ull + uint64_t(C.n) * 131 + uint64_t(C.ngates);
+        for (size_t c = 0; c < count; c++) sig = sig * 1315423911ull + uint64_t(circuits[c].n) * 131 + circuits[c].m;
         key << sig;
     }
     int cl = o.chunk_log2, ct = o.ctas_per_sm;
@@ -607,11 +845,15 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
         }
     }
     if (e == cudaSuccess && (cl <= 0 || ct <= 0)) {
-        // autotune: time one run per candidate
+        // autotune: time one run per candidate (items of 1, 4 or 16 tiles of 2^11 amplitudes)
         double best = 1e30;
-        int bcl = 12, bct = 2;
-        const std::vector<int> cls = cl > 0 ? std::vector<int>{cl} : std::vector<int>{9, 11, 13};
-        const std::vector<int> cts = ct > 0 ? std::vector<int>{ct} : std::vector<int>{2, 4};
+        int bcl = 12, bct = 1;
+        const std::vector<int> cls = cl > 0 ? std::vector<int>{cl} : std::vector<int>{10, 12, 14};
+        std::vector<int> cts;
+        if (ct > 0)
+            cts = {ct};
+        else
+            for (int k = 1; k <= max_per_sm; k++) cts.push_back(k);
         for (int tcl : cls) {
             for (int tct : cts) {
                 b->ctas = tct;
@@ -631,7 +873,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
         ct = bct;
         if (e == cudaSuccess) cache_store(key.str(), cl, ct);
     }
-    b->ctas = std::max(1, ct);
+    b->ctas = std::max(1, std::min(ct, max_per_sm));
     if (e == cudaSuccess) e = layout(std::max(kMinChunk, cl));
     if (e == cudaSuccess) e = capture(b);
     if (e != cudaSuccess) {

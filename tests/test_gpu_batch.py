@@ -14,7 +14,7 @@ def per_circuit(circuits, params, precision):
     off = 0
     for n, gates, npar, terms in circuits:
         reg = q.Register.from_int(n, 0, precision=precision)
-        reg.set_arith(q.QS_ARITH_FMA)
+        reg.set_arith(q.QS_ARITH_FMA)  # FP64 reference for the complex128 forms
         e, g = reg.adjoint_gradient(gates, params[off:off + npar], terms)
         es.append(e)
         gs.append(g)
@@ -22,15 +22,17 @@ def per_circuit(circuits, params, precision):
     return np.array(es), np.concatenate(gs)
 
 
-@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 2e-4)])
-def test_batch_matches_single_circuit_path(precision, tol):
+@pytest.mark.parametrize("precision,arith,tol", [(0, 1, 1e-10), (0, 2, 1e-10), (1, 1, 2e-4)])
+def test_batch_matches_single_circuit_path(precision, arith, tol):
+    """Circuits of 3..13 qubits (one tile up to 11 qubits, several above); items of one tile (cl = 8)
+    and autotuned; arith = 2: complex128 stages in double-float tiles."""
     from quaru_gb300.batch import Batch
     from quaru_gb300.workloads import config5
 
     circuits, params = config5(count=24, qmin=3, qmax=13, lmin=1, lmax=4, seed=99)
     params = np.array(params)
     for cl in (0, 8):
-        b = Batch(circuits, precision=precision, chunk_log2=cl, ctas_per_sm=2 if cl else 0)
+        b = Batch(circuits, precision=precision, chunk_log2=cl, ctas_per_sm=2 if cl else 0, arith=arith)
         e, g = b.run(params)
         e2, g2 = b.run(params)  # graph replay gives the same numbers
         assert np.array_equal(e, e2) and np.array_equal(g, g2)
@@ -42,6 +44,32 @@ def test_batch_matches_single_circuit_path(precision, tol):
     e3, g3 = b.run(p2)
     re3, rg3 = per_circuit(circuits, p2, precision)
     assert np.max(np.abs(g3 - rg3)) < tol
+
+
+@pytest.mark.parametrize("precision,arith,tol", [(0, 1, 1e-10), (0, 2, 1e-10), (1, 1, 2e-4)])
+def test_batch_larger_circuits_fixed_gates(precision, arith, tol):
+    """12..16 qubits with fixed 1-qubit gates mixed in (their stages stay FP64 under DF64): items of
+    1, 4 and 16 tiles."""
+    from quaru_gb300 import ParamGate
+    from quaru_gb300 import operation as O
+    from quaru_gb300.batch import Batch
+    from quaru_gb300.workloads import config5
+
+    circuits, params = config5(count=6, qmin=12, qmax=16, lmin=2, lmax=3, seed=7)
+    mixed = []
+    for i, (n, gates, npar, terms) in enumerate(circuits):
+        g = list(gates)
+        if i % 2:
+            g.insert(len(g) // 2, ParamGate.fixed(O.hadamard(n - 1)))
+            g.insert(len(g) // 3, ParamGate.fixed(O.Operation(np.array([[0, 1j], [1j, 0]]), [0])))
+        mixed.append((n, g, npar, terms))
+    params = np.array(params)
+    re, rg = per_circuit(mixed, params, precision)
+    for cl in (10, 12, 14):
+        b = Batch(mixed, precision=precision, chunk_log2=cl, ctas_per_sm=1, arith=arith)
+        e, g = b.run(params)
+        assert np.max(np.abs(e - re)) < tol
+        assert np.max(np.abs(g - rg)) < tol
 
 
 def test_batch_rejects_unsupported_gates():
