@@ -6,7 +6,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .register import EngineError, OperationError, ParamGate, _check, _dp, _pauli_array, _sp
+from .register import EngineError, OperationError, ParamGate, _check, _dp, _pauli_array, _sp, param_gate_table
 
 
 class Batch:
@@ -19,22 +19,10 @@ class Batch:
         arr = (_lib.QsBatchCircuit * max(1, len(circuits)))()
         self.nparams = []
         for i, (n, gates, nparams, terms) in enumerate(circuits):
-            cg = (_lib.QsParamGate * max(1, len(gates)))()
-            for k, g in enumerate(gates):
-                cg[k].kind = g.kind
-                cg[k].param = g.param
-                if g.kind == _lib.QS_GATE_FIXED:
-                    m = np.ascontiguousarray(np.asarray(g.op.matrix, dtype=np.complex128))
-                    t = np.ascontiguousarray(np.array(list(g.op.targets), dtype=np.uintp))
-                    cg[k].matrix = _dp(m.view(np.float64))
-                    self._keep.append(m)
-                else:
-                    t = np.ascontiguousarray(np.array([g.target], dtype=np.uintp))
-                cg[k].k = len(t)
-                cg[k].targets = _sp(t)
-                self._keep.append(t)
+            table, bufs = param_gate_table(gates)
+            cg = table.ctypes.data_as(ctypes.POINTER(_lib.QsParamGate))
             pt = _pauli_array(terms)
-            self._keep += [cg, pt]
+            self._keep += [table, bufs, pt]
             arr[i].n, arr[i].gates, arr[i].m = n, cg, len(gates)
             arr[i].nparams, arr[i].terms, arr[i].nterms = nparams, pt, len(terms)
             self.nparams.append(nparams)

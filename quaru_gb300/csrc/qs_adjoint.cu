@@ -29,9 +29,9 @@ namespace qs {
 constexpr int kAT = 256;
 
 __device__ __forceinline__ double2 ld2(const double2* p, uint64_t i) { return p[i]; }
-__device__ __forceinline__ double2 ld2(const float2* p, uint64_t i) {
+__device__ __forceinline__ double2 ld2(const float2* p, uint64_t i) {  // integer-pipe conversion
     const float2 v = p[i];
-    return make_double2(double(v.x), double(v.y));
+    return make_double2(df_f2d(v.x), df_f2d(v.y));
 }
 __device__ __forceinline__ void st2(double2* p, uint64_t i, double2 v) { p[i] = v; }
 __device__ __forceinline__ void st2(float2* p, uint64_t i, double2 v) { p[i] = make_float2(float(v.x), float(v.y)); }

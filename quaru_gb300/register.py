@@ -285,31 +285,49 @@ class Register:
 
     def adjoint_gradient(self, gates, params, terms):
         """Energy and gradient of the parameterised circuit `gates` (see ParamGate) for observable `terms`."""
-        n = len(gates)
-        cg = (_lib.QsParamGate * max(1, n))()
-        keep = []
-        for i, g in enumerate(gates):
-            cg[i].kind = g.kind
-            cg[i].param = g.param
-            if g.kind == _lib.QS_GATE_FIXED:
-                m = _matrix(g.op.matrix)
-                t = np.ascontiguousarray(np.array(list(g.op.targets), dtype=np.uintp))
-                cg[i].k = len(t)
-                cg[i].matrix = _dp(m.view(np.float64))
-            else:
-                m = None
-                t = np.ascontiguousarray(np.array([g.target], dtype=np.uintp))
-                cg[i].k = 1
-            cg[i].targets = _sp(t)
-            keep += [m, t]
+        table, keep = param_gate_table(gates)
         p = np.ascontiguousarray(np.asarray(params, dtype=np.float64))
         arr = _pauli_array(terms)
         grad = np.zeros(max(1, p.size), dtype=np.float64)
         e = ctypes.c_double(0)
         err = np.zeros(3, dtype=np.uintp)
-        _check(_lib.load().qs_adjoint_gradient(self._h, cg, n, _dp(p), p.size, arr, len(terms), ctypes.byref(e),
+        _check(_lib.load().qs_adjoint_gradient(self._h, table.ctypes.data_as(ctypes.POINTER(_lib.QsParamGate)),
+                                               len(gates), _dp(p), p.size, arr, len(terms), ctypes.byref(e),
                                                _dp(grad), _sp(err)), err)
+        del keep
         return e.value, grad[: p.size]
+
+
+_PARAM_GATE_DTYPE = np.dtype([("kind", "<i4"), ("param", "<i4"), ("k", "<u8"), ("targets", "<u8"),
+                              ("matrix", "<u8")])  # the layout of qs_param_gate (include/quaru_gpu.h)
+
+
+def param_gate_table(gates):
+    """qs_param_gate records for `gates` as one numpy array (targets and matrices in two shared
+    buffers, addressed by offset): a few array operations per call instead of one ctypes object
+    per gate. Returns (table, buffers to keep alive while the table is in use)."""
+    import itertools
+
+    n = len(gates)
+    fixed = _lib.QS_GATE_FIXED
+    tl = [g.op.targets if g.kind == fixed else (g.target,) for g in gates]
+    ks = np.fromiter((len(t) for t in tl), dtype=np.uint64, count=n)
+    flat = np.fromiter(itertools.chain.from_iterable(tl), dtype=np.uintp, count=int(ks.sum()) if n else 0)
+    if flat.size == 0:
+        flat = np.zeros(1, dtype=np.uintp)
+    table = np.zeros(max(1, n), dtype=_PARAM_GATE_DTYPE)
+    if n:
+        table["kind"][:n] = np.fromiter((g.kind for g in gates), dtype=np.int32, count=n)
+        table["param"][:n] = np.fromiter((g.param for g in gates), dtype=np.int32, count=n)
+        table["k"][:n] = ks
+        table["targets"][:n] = flat.ctypes.data + 8 * (np.cumsum(ks) - ks)
+    fidx = [i for i in range(n) if gates[i].kind == fixed]
+    mats = [np.ascontiguousarray(np.asarray(gates[i].op.matrix, dtype=np.complex128)).ravel() for i in fidx]
+    mflat = np.concatenate(mats) if mats else np.zeros(1, dtype=np.complex128)
+    if fidx:
+        sizes = np.fromiter((m.size for m in mats), dtype=np.uint64, count=len(mats))
+        table["matrix"][fidx] = mflat.ctypes.data + 16 * (np.cumsum(sizes) - sizes)
+    return table, (flat, mflat)
 
 
 class ParamGate:
