@@ -72,6 +72,29 @@ def test_batch_larger_circuits_fixed_gates(precision, arith, tol):
         assert np.max(np.abs(g - rg)) < tol
 
 
+@pytest.mark.parametrize("precision,arith", [(0, 1), (0, 2), (1, 1)])
+def test_batch_tiny_and_mixed_sizes(precision, arith):
+    """1- and 2-qubit circuits (a tile is the whole 2- or 4-amplitude state) next to a 12-qubit one."""
+    from quaru_gb300 import ParamGate
+    from quaru_gb300 import operation as O
+    from quaru_gb300.batch import Batch
+
+    circuits = [
+        (1, [ParamGate.ry(0, 0), ParamGate.rz(0, 1), ParamGate.rx(0, 0)], 2, [(0.7, 0, 1), (0.4, 1, 0)]),
+        (2, [ParamGate.ry(0, 0), ParamGate.ry(1, 1), ParamGate.fixed(O.cnot(0, 1)), ParamGate.rz(1, 2),
+             ParamGate.fixed(O.hadamard(0))], 3, [(1.1, 0, 3), (-0.3, 2, 0), (0.5, 3, 3)]),
+        (12, [ParamGate.ry(q, q) for q in range(12)] + [ParamGate.fixed(O.cnot(q, q + 1)) for q in range(11)]
+         + [ParamGate.rz(q, 12 + q) for q in range(12)], 24, [(0.9, 0, 0b11), (0.6, 1 << 11, 0)]),
+    ]
+    params = np.random.default_rng(5).uniform(0, 2 * np.pi, size=2 + 3 + 24)
+    tol = 1e-10 if precision == 0 else 2e-4
+    re, rg = per_circuit(circuits, params, precision)
+    b = Batch(circuits, precision=precision, arith=arith)
+    e, g = b.run(params)
+    assert np.max(np.abs(e - re)) < tol
+    assert np.max(np.abs(g - rg)) < tol
+
+
 def test_batch_rejects_unsupported_gates():
     import quaru_gb300 as q
     from quaru_gb300 import ParamGate
