@@ -63,6 +63,42 @@ __device__ __forceinline__ void pv_dense(const float* u, int fm, int fv, float2 
     }
 }
 
+// As pv_dense (no controls), on registers relabelled across bit J when `flip`: physical register
+// a | 1 << J then holds logical row 0, so the gate runs with rows and columns exchanged.
+template <int J>
+__device__ __forceinline__ void pv_dense_flip(const float* u, bool flip, float2 (&x)[16]) {
+    float4 c0 = *reinterpret_cast<const float4*>(u), c1 = *reinterpret_cast<const float4*>(u + 4);
+    if (flip) {  // (u00, u01; u10, u11) -> (u11, u10; u01, u00)
+        const float4 t0 = make_float4(c1.z, c1.w, c1.x, c1.y), t1 = make_float4(c0.z, c0.w, c0.x, c0.y);
+        c0 = t0;
+        c1 = t1;
+    }
+#pragma unroll
+    for (int a = 0; a < 16; a++) {
+        if (a & (1 << J)) continue;
+        const int b = a | (1 << J);
+        const float2 xa = x[a], xb = x[b];
+        float2 y0 = cfma(c0.z, c0.w, xb, czero<float2>());
+        y0 = cfma(c0.x, c0.y, xa, y0);
+        float2 y1 = cfma(c1.z, c1.w, xb, czero<float2>());
+        y1 = cfma(c1.x, c1.y, xa, y1);
+        x[a] = y0;
+        x[b] = y1;
+    }
+}
+
+// Physical exchange of the registers across bit J (materialises a relabelling).
+template <int J>
+__device__ __forceinline__ void pv_xswap(float2 (&x)[16]) {
+#pragma unroll
+    for (int a = 0; a < 16; a++) {
+        if (a & (1 << J)) continue;
+        const float2 t = x[a];
+        x[a] = x[a | (1 << J)];
+        x[a | (1 << J)] = t;
+    }
+}
+
 template <int J, bool ALL>
 __device__ __forceinline__ void pv_real(const float* u, int fm, int fv, float2 (&x)[16]) {
     const float4 c = *reinterpret_cast<const float4*>(u);
@@ -102,12 +138,13 @@ __device__ __forceinline__ void pv_mono(const float* u, int fm, int fv, float2 (
     }
 }
 
-// Swap on register bit J where register bit C is 1 (CNOT with both qubits in registers).
-template <int J, int C>
+// Swap on register bit J where register bit C is V (CNOT with both qubits in registers; V = 0 when
+// the registers are relabelled across bit C).
+template <int J, int C, int V = 1>
 __device__ __forceinline__ void pv_swapc(float2 (&x)[16]) {
 #pragma unroll
     for (int a = 0; a < 16; a++) {
-        if ((a & (1 << J)) || !(a & (1 << C))) continue;
+        if ((a & (1 << J)) || (((a >> C) & 1) != V)) continue;
         const int b = a | (1 << J);
         const float2 t = x[a];
         x[a] = x[b];
@@ -192,22 +229,43 @@ __device__ __forceinline__ void pv_phase(const float* u, int fm, int fv, float2 
 // of bit tests: a large switch costs about a hundred extra instructions per gate on sm_103a.
 // COMMON: only the variants pass_common() admits are compiled (fewer live registers; the stage
 // kernel with a copy warp runs at 96 registers per thread).
+//
+// COMMON also relabels registers: a swap without register controls toggles bit J of xm (logical
+// register l lives in physical register l ^ xm) instead of moving data; register gates read xm
+// (rows exchanged, control values adjusted), lane gates materialise it first (partners must agree),
+// and the pass stores register p at the offset of p ^ xm.
 template <bool COMMON>
-__device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t base, float2 (&x)[16]) {
+__device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t base, float2 (&x)[16],
+                                         uint32_t& xm) {
     const PassMember& g = m->pm;
     const uint32_t vid = ctl & 255u, cat = vid >> 4, low = vid & 15u;
     if (cat == PV_DENSES) {  // 1..4 dense gates without controls, one entry each
         int e = 0;
-        if (low & 1u) pv_dense<0, true>(m[e++].pm.u, 0, 0, x);
-        if (low & 2u) pv_dense<1, true>(m[e++].pm.u, 0, 0, x);
-        if (low & 4u) pv_dense<2, true>(m[e++].pm.u, 0, 0, x);
-        if (low & 8u) pv_dense<3, true>(m[e++].pm.u, 0, 0, x);
+        if (COMMON) {
+            if (low & 1u) pv_dense_flip<0>(m[e++].pm.u, xm & 1u, x);
+            if (low & 2u) pv_dense_flip<1>(m[e++].pm.u, xm & 2u, x);
+            if (low & 4u) pv_dense_flip<2>(m[e++].pm.u, xm & 4u, x);
+            if (low & 8u) pv_dense_flip<3>(m[e++].pm.u, xm & 8u, x);
+        } else {
+            if (low & 1u) pv_dense<0, true>(m[e++].pm.u, 0, 0, x);
+            if (low & 2u) pv_dense<1, true>(m[e++].pm.u, 0, 0, x);
+            if (low & 4u) pv_dense<2, true>(m[e++].pm.u, 0, 0, x);
+            if (low & 8u) pv_dense<3, true>(m[e++].pm.u, 0, 0, x);
+        }
         return;
     }
     const bool on = !(ctl & (1u << 13)) || (base & g.om) == g.ov;
-    const int fm = g.fmv & 15, fv = (g.fmv >> 4) & 15;
+    const int fm = g.fmv & 15;
+    const int fv = ((g.fmv >> 4) & 15) ^ int(xm & uint32_t(fm));  // controls read through the relabelling
     const bool all = low & 2u, nocond = low & 1u;
     if (cat == PV_LDENSE || cat == PV_LSWAP) {  // lane gates: every lane takes part in the shuffles
+        if (COMMON && xm) {
+            if (xm & 1u) pv_xswap<0>(x);
+            if (xm & 2u) pv_xswap<1>(x);
+            if (xm & 4u) pv_xswap<2>(x);
+            if (xm & 8u) pv_xswap<3>(x);
+            xm = 0;
+        }
 #define QS_PV_LANE(C)                                                          \
     {                                                                          \
         if (all) {                                                             \
@@ -230,6 +288,10 @@ __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t
     }
     if (!on) return;  // register and phase gates: this tuple fails the controls
     if (cat == PV_SWAP) {
+        if (COMMON && all) {  // relabel instead of moving
+            xm ^= 1u << (low >> 2);
+            return;
+        }
 #define QS_PV_SW(J) \
     if (all) pv_mono<J, PC_SWAP, true>(g.u, fm, fv, x); else pv_mono<J, PC_SWAP, false>(g.u, fm, fv, x)
         QS_PV_J4(low, 2, QS_PV_SW)
@@ -237,16 +299,23 @@ __device__ __forceinline__ void pv_apply(const TileOp* m, uint32_t ctl, uint32_t
         return;
     }
     if (cat == PV_SWAPC) {
-#define QS_PV_SC(J)                                            \
-    {                                                          \
-        const uint32_t c = low & 3u;                           \
-        if (c == 0) pv_swapc<J, (J == 0 ? 1 : 0)>(x);          \
-        else if (c == 1) pv_swapc<J, (J == 1 ? 0 : 1)>(x);     \
-        else if (c == 2) pv_swapc<J, (J == 2 ? 0 : 2)>(x);     \
-        else pv_swapc<J, (J == 3 ? 0 : 3)>(x);                 \
+        const uint32_t c = low & 3u;
+        const bool v0 = COMMON && ((xm >> c) & 1u);  // the control bit is relabelled: it reads 1 where it holds 0
+#define QS_PV_SC1(J, CC)                              \
+    {                                                 \
+        if (v0) pv_swapc<J, CC, 0>(x);                \
+        else pv_swapc<J, CC, 1>(x);                   \
+    }
+#define QS_PV_SC(J)                                   \
+    {                                                 \
+        if (c == 0) QS_PV_SC1(J, (J == 0 ? 1 : 0))    \
+        else if (c == 1) QS_PV_SC1(J, (J == 1 ? 0 : 1)) \
+        else if (c == 2) QS_PV_SC1(J, (J == 2 ? 0 : 2)) \
+        else QS_PV_SC1(J, (J == 3 ? 0 : 3))           \
     }
         QS_PV_J4(low, 2, QS_PV_SC)
 #undef QS_PV_SC
+#undef QS_PV_SC1
         return;
     }
     if (cat == PV_PHASE) {
@@ -302,14 +371,18 @@ __device__ __forceinline__ void pass_run_c64(float2* s, uint32_t tsize, const ui
         float2 x[16];
 #pragma unroll
         for (int j = 0; j < 16; j++) x[j] = sb[off(j)];
+        uint32_t xm = 0;  // register relabelling (COMMON only)
         for (int mi = 1; mi <= cnt;) {
             const TileOp* m = hdr + mi;
             const uint32_t ctl = m->pm.ctl;
-            if (!(ctl & (1u << 12)) || (*tile_base & m->omask) == m->oval) pv_apply<COMMON>(m, ctl, base, x);
+            if (!(ctl & (1u << 12)) || (*tile_base & m->omask) == m->oval) pv_apply<COMMON>(m, ctl, base, x, xm);
             mi += int((ctl >> 8) & 3u) + 1;
         }
+        // physical register j holds logical register j ^ xm: its offset is off(j) ^ off(xm)
+        const uint32_t offx = off(0) ^ (((xm & 1u) ? hdr->off[1] : 0u) ^ ((xm & 2u) ? hdr->off[2] : 0u) ^
+                                        ((xm & 4u) ? hdr->off[4] : 0u) ^ ((xm & 8u) ? hdr->offsrc[0] : 0u));
 #pragma unroll
-        for (int j = 0; j < 16; j++) sb[off(j)] = x[j];
+        for (int j = 0; j < 16; j++) sb[off(j) ^ offx] = x[j];
     }
 }
 
