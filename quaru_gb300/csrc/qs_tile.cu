@@ -196,7 +196,14 @@ __device__ __forceinline__ void dense_pair(const DenseCoef<0>& c, bool real, dou
     a = y0;
     b = y1;
 }
-__device__ __forceinline__ void dense_pair(const DenseCoef<1>& c, bool, double2& a, double2& b) {
+__device__ __forceinline__ void dense_pair(const DenseCoef<1>& c, bool real, double2& a, double2& b) {
+    if (real) {  // real matrix (H, RY): 2 FMAs per output component instead of 4
+        const double2 y0 = cfma_real(c.m[0], a, cfma_real(c.m[2], b, czero<double2>()));
+        const double2 y1 = cfma_real(c.m[4], a, cfma_real(c.m[6], b, czero<double2>()));
+        a = y0;
+        b = y1;
+        return;
+    }
     double2 y0 = cfma(c.m[2], c.m[3], b, czero<double2>());
     y0 = cfma(c.m[0], c.m[1], a, y0);
     double2 y1 = cfma(c.m[6], c.m[7], b, czero<double2>());
