@@ -403,10 +403,84 @@ static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exac
     return counted(cudaGetLastError());
 }
 
+// Dense k-qubit gate (k = 2, 3) on complex128 state in double-float arithmetic (QS_ARITH_DF64):
+// each output component is one double-float dot product over the 2^(k+1) real terms of its row,
+// rounded once to FP64 (df_dot). The amplitudes are split into float pairs with integer operations.
+template <int K>
+struct DenseKDfArgs {
+    IndexMap map;
+    uint64_t off[1 << K];
+    float reh[1 << K][2 << K], rel[1 << K][2 << K];  // row r, real part: terms over (x.re[0..D), x.im[0..D))
+    float imh[1 << K][2 << K], iml[1 << K][2 << K];  // row r, imaginary part: terms over (x.im[0..D), x.re[0..D))
+};
+
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_denseK_df(double2* __restrict__ st, uint64_t ntup,
+                                                        const __grid_constant__ DenseKDfArgs<K> a) {
+    constexpr int D = 1 << K;
+    const uint64_t stride = uint64_t(gridDim.x) * kThreads;
+    for (uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x; t < ntup; t += stride) {
+        const uint64_t base = expand_index(t, a.map);
+        float xh[2 * D], xl[2 * D], ph[2 * D], pl[2 * D];  // (re, im) and (im, re) orders
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            const double2 v = st[base + a.off[c]];
+            df_split(v.x, xh[c], xl[c]);
+            df_split(v.y, xh[D + c], xl[D + c]);
+            ph[c] = xh[D + c];
+            pl[c] = xl[D + c];
+            ph[D + c] = xh[c];
+            pl[D + c] = xl[c];
+        }
+#pragma unroll 1
+        for (int r = 0; r < D; r++) {
+            const double re = df_dot<2 * D>(a.reh[r], a.rel[r], xh, xl);
+            const double im = df_dot<2 * D>(a.imh[r], a.iml[r], ph, pl);
+            st[base + a.off[r]] = make_double2(re, im);
+        }
+    }
+}
+
+// The double-float coefficients of a dense k-qubit matrix; false when an entry is outside the
+// range double-float handles (the FP64 kernel runs instead).
+template <int K>
+static bool fill_denseK_df(const OpDesc& op, DenseKDfArgs<K>& a) {
+    constexpr int D = 1 << K;
+    auto split = [](double v, float& h, float& l) {
+        const double av = v < 0 ? -v : v;
+        if (av != 0.0 && (av > 0x1p100 || av < 0x1p-100)) return false;
+        h = float(v);
+        l = float(v - double(h));
+        return true;
+    };
+    for (int r = 0; r < D; r++)
+        for (int c = 0; c < D; c++) {
+            const double mr = op.m[2 * (r * D + c)], mi = op.m[2 * (r * D + c) + 1];
+            if (!split(mr, a.reh[r][c], a.rel[r][c]) || !split(-mi, a.reh[r][D + c], a.rel[r][D + c]) ||
+                !split(mr, a.imh[r][c], a.iml[r][c]) || !split(mi, a.imh[r][D + c], a.iml[r][D + c]))
+                return false;
+        }
+    return true;
+}
+
 template <typename R, int K>
-static cudaError_t launch_denseK(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms) {
+static cudaError_t launch_denseK(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms,
+                                 bool df64 = false) {
     using T = typename Cplx<R>::T;
     constexpr int D = 1 << K;
+    if constexpr (sizeof(R) == 8 && K <= 3) {
+        if (df64) {
+            DenseKDfArgs<K> d;
+            std::memset(&d, 0, sizeof(d));
+            if (fill_denseK_df<K>(op, d)) {
+                d.map = make_map(op);
+                for (int j = 0; j < D; j++) d.off[j] = sub_offset(op, j);
+                const uint64_t ntup = 1ull << (n - K - __builtin_popcountll(op.fixmask));
+                k_denseK_df<K><<<grid_for(ntup, sms), kThreads, 0, s>>>(static_cast<double2*>(state), ntup, d);
+                return counted(cudaGetLastError());
+            }
+        }
+    }
     DenseKArgs<R, K> a;
     std::memset(&a, 0, sizeof(a));
     a.map = make_map(op);
@@ -480,8 +554,8 @@ static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact
                 return launch_mono<R, 0>(z, state, n, s, sms);
             }
             case 1: return launch_dense1<R>(op, state, n, exact, s, sms, df64);
-            case 2: return launch_denseK<R, 2>(op, state, n, exact, s, sms);
-            case 3: return launch_denseK<R, 3>(op, state, n, exact, s, sms);
+            case 2: return launch_denseK<R, 2>(op, state, n, exact, s, sms, df64);
+            case 3: return launch_denseK<R, 3>(op, state, n, exact, s, sms, df64);
             case 4: return launch_denseK<R, 4>(op, state, n, exact, s, sms);
             case 5: return launch_denseK<R, 5>(op, state, n, exact, s, sms);
         }

@@ -327,6 +327,24 @@ def test_df64_random_circuits_within_tolerance(q, orc, n):
     assert floored_rel_err(g, o) <= 1e-12
 
 
+def test_df64_dense_multi_qubit_gates(q, orc):
+    """DF64: dense 2- and 3-qubit gates (double-float kernel), their controlled forms, and 4-qubit
+    gates (FP64 kernel), 60 gates deep, within the 1e-12 floored bound of the FP64 oracle."""
+    from quaru_gb300 import operation as O
+    from quaru_gb300.operation import Operation
+
+    rng = np.random.default_rng(320)
+    n = 12
+    ops = []
+    for i in range(60):
+        k = (2, 3, 2, 3, 4)[i % 5]
+        tg = [int(x) for x in rng.permutation(n)[:k + 1]]
+        g = Operation(rand_unitary(rng, k), tg[:k])
+        ops.append(O.to_controlled(g, tg[k]) if i % 7 == 3 else g)
+    o, g = run_pair(q, orc, n, ops, arith=2, state=rand_state(rng, n))
+    assert floored_rel_err(g, o) <= 1e-12
+
+
 def test_df64_deep_layered_circuit(q, orc):
     from quaru_gb300.workloads import flatten, layered_circuit
 
