@@ -863,6 +863,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
                 const auto t0 = std::chrono::steady_clock::now();
                 cudaGraphLaunch(b->exec, b->stream);
                 e = cudaStreamSynchronize(b->stream);
+                note_launches(6);
                 const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
                 if (e != cudaSuccess || *b->herr) break;
                 if (dt < best) best = dt, bcl = tcl, bct = tct;
@@ -898,6 +899,7 @@ extern "C" int qs_batch_run(qs_batch* b, const double* params, double* energies,
         b->hcs[i] = make_double2(std::cos(0.5 * th), std::sin(0.5 * th));
     }
     cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+    if (e == cudaSuccess) note_launches(3);  // the graph's reset, persistent and reduction kernels
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
         set_last_error_message(std::string("batch run: ") + cudaGetErrorString(e));
