@@ -176,6 +176,8 @@ struct AdjOpDev {
     int pad_[2];
 };
 
+static_assert(sizeof(AdjOpDev) % 16 == 0, "the op table is copied to shared memory in 16-byte words");
+
 struct AdjStageArgs {
     int T, RL, RH;
     int nops, nrot;
@@ -229,8 +231,10 @@ __device__ __forceinline__ void adj_fixed(T* s, const TileOp& op, uint32_t tsize
     }
 }
 
+// The rotation un-applied from both tiles; returns this thread's share of Im<lambda|A|psi> (complex128:
+// an FP64 sum; complex64: a compensated float pair).
 template <typename T, int AXIS>
-__device__ __forceinline__ double adj_rot_tile(T* sp, T* sl, const AdjOpDev& op, uint32_t tsize) {
+__device__ __forceinline__ auto adj_rot_tile(T* sp, T* sl, const AdjOpDev& op, uint32_t tsize) {
     using R = decltype(T().x);
     const TileOp& t = op.t;
     uint32_t seg[5];
@@ -254,8 +258,10 @@ __device__ __forceinline__ double adj_rot_tile(T* sp, T* sl, const AdjOpDev& op,
         sl[i0] = l0;
         sl[i1] = l1;
     }
-    if constexpr (sizeof(R) == 4) acc = __dadd_rn(df_f2d(facc.s), df_f2d(facc.c));
-    return acc;
+    if constexpr (sizeof(R) == 4)
+        return facc;
+    else
+        return acc;
 }
 
 template <int AXIS>
@@ -322,9 +328,16 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
     float4* fp = reinterpret_cast<float4*>(sp);  // the same buffers as double-float amplitudes
     float4* fl = reinterpret_cast<float4*>(sl);
     double* sacc = reinterpret_cast<double*>(sl + tsize);  // [nrot][8 warps]
-    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sacc + size_t(a.nrot) * (kAdjThreads / 32));
+    AdjOpDev* sops = reinterpret_cast<AdjOpDev*>(sacc + size_t(a.nrot) * (kAdjThreads / 32));
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sops + a.nops);
     const int nrows = 1 << a.RH, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < a.nrot * (kAdjThreads / 32); i += kAdjThreads) sacc[i] = 0.0;
+    {  // the launch's op table, read by every thread for every gate of every tile
+        const uint4* src = reinterpret_cast<const uint4*>(ops);
+        uint4* dst = reinterpret_cast<uint4*>(sops);
+        const int words = a.nops * int(sizeof(AdjOpDev) / 16);
+        for (int w = threadIdx.x; w < words; w += kAdjThreads) dst[w] = src[w];
+    }
     for (int r = threadIdx.x; r < nrows; r += kAdjThreads) {
         uint64_t o = 0;
         for (int b = 0; b < a.RH; b++)
@@ -353,7 +366,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
         }
         __syncthreads();
         for (int o = 0; o < a.nops; o++) {
-            const AdjOpDev& op = ops[o];
+            const AdjOpDev& op = sops[o];
             if ((base & op.t.omask) != op.t.oval) continue;  // the same for the whole block
             if (op.rot >= 0) {
                 double v;
@@ -364,6 +377,19 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
                         v = adj_rot_tile_df<QS_GATE_RY>(fp, fl, op, tsize);
                     else
                         v = adj_rot_tile_df<QS_GATE_RZ>(fp, fl, op, tsize);
+                    v = rd_warp_sum(v);
+                } else if constexpr (sizeof(T) == 8) {
+                    // complex64: the warp's compensated float pairs reduced on the FP32 pipe, one
+                    // FP64 rejoin per warp
+                    DfAcc f;
+                    if (op.axis == QS_GATE_RX)
+                        f = adj_rot_tile<T, QS_GATE_RX>(sp, sl, op, tsize);
+                    else if (op.axis == QS_GATE_RY)
+                        f = adj_rot_tile<T, QS_GATE_RY>(sp, sl, op, tsize);
+                    else
+                        f = adj_rot_tile<T, QS_GATE_RZ>(sp, sl, op, tsize);
+                    f.warp_reduce();
+                    v = __dadd_rn(df_f2d(f.s), df_f2d(f.c));
                 } else {
                     if (op.axis == QS_GATE_RX)
                         v = adj_rot_tile<T, QS_GATE_RX>(sp, sl, op, tsize);
@@ -371,9 +397,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
                         v = adj_rot_tile<T, QS_GATE_RY>(sp, sl, op, tsize);
                     else
                         v = adj_rot_tile<T, QS_GATE_RZ>(sp, sl, op, tsize);
+                    v = rd_warp_sum(v);
                 }
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
                 if (lane == 0) sacc[op.rot * (kAdjThreads / 32) + warp] += v;
             } else if constexpr (DF) {
                 adj_move_df(fp, op.t, tsize);
@@ -519,18 +544,13 @@ static std::vector<double> rotation_matrix(int axis, double c, double s) {
 // Grid of the tiled reverse sweep for n qubits (the same for every stage, so partials line up).
 template <typename T>
 static int adj_grid(int n, int sms) {
-    const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 + (8u << 6);
-    if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_adj_stage<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (sizeof(T) == 16)
-            cudaFuncSetAttribute(k_adj_stage<T, sizeof(T) == 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(smem));
-    }
-    int per_sm = 1;  // the smaller of the two variants' occupancies
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_stage<T, false>, kAdjThreads, smem);
+    const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 +
+                        size_t(kMaxStageOps) * sizeof(AdjOpDev) + (8u << 6);
+    int per_sm = 1;  // the smaller of the two variants' occupancies (each variant's limit raised to smem)
+    resident_blocks(reinterpret_cast<const void*>(k_adj_stage<T, false>), kAdjThreads, smem, &per_sm);
     if (sizeof(T) == 16) {
         int df = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&df, k_adj_stage<T, sizeof(T) == 16>, kAdjThreads, smem);
+        resident_blocks(reinterpret_cast<const void*>(k_adj_stage<T, sizeof(T) == 16>), kAdjThreads, smem, &df);
         per_sm = std::min(per_sm, df);
     }
     const uint64_t ntiles = 1ull << (n - kAdjT);
@@ -634,7 +654,8 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
         a.nops = L.count;
         a.nrot = L.nrot;
         for (int r = 0; r < L.nrot; r++) a.slot[r] = L.slot[r];
-        const size_t smem = 2 * (sizeof(T) << st.T) + size_t(a.nrot) * (kAdjThreads / 32) * 8 + (8u << a.RH);
+        const size_t smem = 2 * (sizeof(T) << st.T) + size_t(a.nrot) * (kAdjThreads / 32) * 8 +
+                            size_t(a.nops) * sizeof(AdjOpDev) + (8u << a.RH);
         if (sizeof(T) == 16 && L.moves_only && arith == QS_ARITH_DF64)
             k_adj_stage<T, sizeof(T) == 16><<<grid, kAdjThreads, smem, s>>>((T*)state, (T*)lam, ntiles, a,
                                                                            dops + L.first, part);

@@ -9,8 +9,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "qs_adjoint.h"
@@ -34,6 +37,34 @@ struct qs_register {
 namespace qs {
 static std::atomic<uint64_t> g_launches{0};
 void note_launches(uint64_t count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+
+cudaError_t resident_blocks(const void* func, int threads, size_t smem, int* per_sm) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;                     // dynamic smem limit set
+    static std::map<std::tuple<int, const void*, int, size_t>, int> occupancy;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(dev, func, threads, smem);
+    const auto hit = occupancy.find(key);
+    if (hit != occupancy.end()) {
+        *per_sm = hit->second;
+        return cudaSuccess;
+    }
+    size_t& lim = limit[std::make_pair(dev, func)];
+    if (smem > 48 * 1024 && smem > lim) {
+        e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        lim = smem;
+    }
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, func, threads, smem);
+    if (e != cudaSuccess) return e;
+    occupancy[key] = n;
+    *per_sm = n;
+    return cudaSuccess;
+}
 }  // namespace qs
 
 namespace {

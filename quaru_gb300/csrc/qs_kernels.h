@@ -15,6 +15,12 @@ constexpr uint8_t PF_SKIP_DEV = 4;  // PfClass::PF_SKIP as seen by device code
 // Count kernel launches made by this library (read back through qs_launch_count).
 void note_launches(uint64_t count);
 
+// Resident blocks per SM of kernel `func` at `threads` threads and `smem` bytes of dynamic shared
+// memory, raising the kernel's dynamic shared memory limit to `smem` first where needed. Both the
+// limit and the occupancy are remembered per device, kernel and size, so a launcher pays for the
+// two runtime queries once.
+cudaError_t resident_blocks(const void* func, int threads, size_t smem, int* per_sm);
+
 // Set the message qs_last_error() returns on the calling thread.
 void set_last_error_message(const std::string& msg);
 

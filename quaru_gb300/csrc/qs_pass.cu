@@ -207,10 +207,8 @@ cudaError_t launch_pass(void* state, int n, const TileStage& st, int op_begin, i
     const size_t smem = size_t(pa.nbuf) * tile_bytes + fixed;
     const uint64_t ntiles = 1ull << (n - st.T);
     auto go = [&](auto kern, int nthreads) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
         int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nthreads, smem);
+        cudaError_t e = resident_blocks(reinterpret_cast<const void*>(kern), nthreads, smem, &per_sm);
         if (e != cudaSuccess) return e;
         const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm)));
         kern<<<int(grid), nthreads, smem, s>>>(static_cast<float2*>(state), ntiles, pa, dops, derr);

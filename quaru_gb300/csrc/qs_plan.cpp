@@ -102,35 +102,35 @@ TileOp make_tile_op(const OpDesc& op, const TileStage& st) {
     };
     t.kind = uint8_t(op.kind);
     t.k = uint8_t(op.k);
-    std::vector<int> pos;
+    int pos[72], npos = 0;  // targets (k <= 5) and fixed bits (< 64)
     for (int j = 0; j < op.k; j++) {
         t.tb[j] = uint8_t(local(op.tq[j]));
-        pos.push_back(t.tb[j]);
+        pos[npos++] = t.tb[j];
     }
-    for (int b = 0; b < 64; b++) {
-        if (!(op.fixmask >> b & 1ull)) continue;
+    for (uint64_t fm = op.fixmask; fm; fm &= fm - 1) {
+        const int b = __builtin_ctzll(fm);
         const int lb = local(b);
         const bool one = (op.fixval >> b) & 1ull;
         if (lb >= 0) {
-            pos.push_back(lb);
+            pos[npos++] = lb;
             if (one) t.lfixval |= 1u << lb;
         } else {
             t.omask |= 1ull << b;
             if (one) t.oval |= 1ull << b;
         }
     }
-    std::sort(pos.begin(), pos.end());
-    t.npos = uint8_t(pos.size());
-    for (size_t i = 0; i < pos.size() && i < 16; i++) t.pos[i] = uint8_t(pos[i]);
-    if (pos.size() <= 4) {
+    std::sort(pos, pos + npos);
+    t.npos = uint8_t(npos);
+    for (int i = 0; i < npos && i < 16; i++) t.pos[i] = uint8_t(pos[i]);
+    if (npos <= 4) {
         // Segment j of the expanded index holds the bits between the (j-1)-th and
         // j-th inserted zero; tuple bits land there shifted left by j.
         int lo = 0;
-        for (size_t j = 0; j <= pos.size(); j++) {
-            const int hi = (j < pos.size()) ? pos[j] : 32;
-            uint32_t m = 0;
-            for (int b = lo; b < hi && b < 32; b++) m |= 1u << b;
-            t.seg[j] = m;
+        for (int j = 0; j <= npos; j++) {
+            const int hi = (j < npos) ? pos[j] : 32;
+            const uint64_t below_hi = (hi >= 32) ? 0xffffffffull : ((1ull << hi) - 1ull);
+            const uint64_t below_lo = (lo >= 32) ? 0xffffffffull : ((1ull << lo) - 1ull);
+            t.seg[j] = uint32_t(below_hi & ~below_lo);
             lo = hi + 1;
         }
     }
@@ -233,8 +233,8 @@ static TileOp pass_header(const int (&r)[kPassBits], int entries) {
     return h;
 }
 
-// Member entry of a pass gate t (a tile op of kind dense / monomial, k <= 1) for register bits r.
-static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
+// Fills the member fields of pass gate t (a tile op of kind dense / monomial, k <= 1) for register bits r.
+static void pass_member(TileOp& t, const int (&r)[kPassBits]) {
     auto rix = [&](int lb) -> int {
         for (int i = 0; i < kPassBits; i++)
             if (r[i] == lb) return i;
@@ -305,7 +305,6 @@ static TileOp pass_member(TileOp t, const int (&r)[kPassBits]) {
         }
     }
     pm.ctl = vid | (lane << 10) | (t.omask ? (1u << 12) : 0u) | (pm.om ? (1u << 13) : 0u);
-    return t;
 }
 
 // Whether member entry e is a single dense gate on a register bit with no controls of any kind.
@@ -318,38 +317,38 @@ static bool plain_dense(const TileOp& e, int* J) {
 
 // Emits a pass: header, then the members with runs of plain dense gates on distinct register bits
 // merged into one multi-gate entry (bits in increasing order; such gates commute).
-static void emit_pass(const int (&r)[kPassBits], const std::vector<TileOp>& members, std::vector<TileOp>& prog) {
-    std::vector<TileOp> out;
+static void emit_pass(const int (&r)[kPassBits], const std::vector<TileOp>& tops, const std::vector<int>& members,
+                      std::vector<TileOp>& prog) {
+    const size_t head_at = prog.size();
+    prog.push_back(pass_header(r, 0));
     for (size_t i = 0; i < members.size();) {
         int J;
-        if (!plain_dense(members[i], &J)) {
-            out.push_back(members[i++]);
+        if (!plain_dense(tops[members[i]], &J)) {
+            prog.push_back(tops[members[i++]]);
             continue;
         }
         uint32_t mask = 0;
-        std::vector<const TileOp*> byj(kPassBits, nullptr);
+        int byj[kPassBits] = {-1, -1, -1, -1};
         size_t k = i;
-        while (k < members.size() && plain_dense(members[k], &J) && !(mask >> J & 1u)) {
+        while (k < members.size() && plain_dense(tops[members[k]], &J) && !(mask >> J & 1u)) {
             mask |= 1u << J;
-            byj[J] = &members[k];
+            byj[J] = members[k];
             k++;
         }
         if (__builtin_popcount(mask) < 2) {
-            out.push_back(members[i++]);
+            prog.push_back(tops[members[i++]]);
             continue;
         }
         bool head = true;
         for (int j = 0; j < kPassBits; j++) {
-            if (!byj[j]) continue;
-            TileOp e = *byj[j];
-            if (head) e.pm.ctl = (PV_DENSES << 4) | mask | (uint32_t(__builtin_popcount(mask) - 1) << 8);
+            if (byj[j] < 0) continue;
+            prog.push_back(tops[byj[j]]);
+            if (head) prog.back().pm.ctl = (PV_DENSES << 4) | mask | (uint32_t(__builtin_popcount(mask) - 1) << 8);
             head = false;
-            out.push_back(e);
         }
         i = k;
     }
-    prog.push_back(pass_header(r, int(out.size())));
-    for (const TileOp& e : out) prog.push_back(e);
+    prog[head_at].k = uint8_t(prog.size() - head_at - 1);
 }
 
 static uint64_t op_qubits(const OpDesc& op) {
@@ -377,39 +376,89 @@ static void schedule_passes(const std::vector<OpDesc>& ops, const TileStage& st,
     std::vector<int> upper;
     for (int b = kLaneBits; b < st.T; b++) upper.push_back(b);
     const int U = int(upper.size());
+    // need[i]: the upper tile bit gate i's target must hold as a register bit (0: a lane bit or none)
+    std::vector<uint32_t> need(m, 0u);
+    for (int i = 0; i < m; i++)
+        if (tgt[i] >= kLaneBits) need[i] = 1u << (tgt[i] - kLaneBits);
+    // the gates a choice c of register bits (a mask over `upper`) lets run in this pass, over the
+    // gates not yet scheduled (live, in order): branch-free, it runs for every choice of 4 bits
+    std::vector<int> live;
+    std::vector<uint32_t> lneed;
+    std::vector<uint64_t> lqm;
+    std::vector<uint64_t> cand;
+    auto runnable = [&](uint32_t c) {
+        uint64_t blocked = 0;
+        int count = 0;
+        const size_t nl = live.size();
+        for (size_t i = 0; i < nl; i++) {
+            const bool ok = !(lneed[i] & ~c) && !(lqm[i] & blocked);
+            count += ok;
+            blocked |= ok ? 0ull : lqm[i];
+        }
+        return count;
+    };
     while (left > 0) {
-        int best_count = -1, best_r[kPassBits] = {0, 0, 0, 0};
-        std::vector<int> best_sel;
+        live.clear();
+        lneed.clear();
+        lqm.clear();
+        for (int i = 0; i < m; i++)
+            if (!done[i]) {
+                live.push_back(i);
+                lneed.push_back(need[i]);
+                lqm.push_back(qm[i]);
+            }
+        // Exhaustive over the choices, in order of an upper bound (the gates whose targets a choice
+        // holds, blocked or not); the first choice with the most runnable gates wins, as in a plain
+        // scan over c, and no choice whose bound cannot beat (or tie at a smaller c) is evaluated.
+        int cnt0 = 0, cnt[32] = {0};
+        for (size_t i = 0; i < live.size(); i++) {
+            if (lneed[i])
+                cnt[__builtin_ctz(lneed[i])]++;
+            else
+                cnt0++;
+        }
+        cand.clear();
         for (uint32_t c = 0; c < (1u << U); c++) {
             if (__builtin_popcount(c) != kPassBits) continue;
-            int r[kPassBits], ri = 0;
-            for (int i = 0; i < U; i++)
-                if (c >> i & 1u) r[ri++] = upper[i];
-            uint64_t blocked = 0;
-            std::vector<int> sel;
-            for (int i = 0; i < m; i++) {
-                if (done[i]) continue;
-                bool fits = tgt[i] < kLaneBits;
-                for (int j = 0; j < kPassBits && !fits; j++) fits = (r[j] == tgt[i]);
-                if (!fits || (qm[i] & blocked)) {
-                    blocked |= qm[i];
-                    continue;
-                }
-                sel.push_back(i);
+            int ub = cnt0;
+            for (uint32_t x = c; x; x &= x - 1) ub += cnt[__builtin_ctz(x)];
+            cand.push_back((uint64_t(uint32_t(~ub)) << 32) | c);  // bound descending, then c ascending
+        }
+        std::sort(cand.begin(), cand.end());
+        int best_count = -1;
+        uint32_t best_c = 0;
+        for (uint64_t key : cand) {
+            const int ub = int(~uint32_t(key >> 32));
+            const uint32_t c = uint32_t(key);
+            if (ub < best_count || (ub == best_count && c > best_c)) {
+                if (ub < best_count) break;
+                continue;
             }
-            if (int(sel.size()) > best_count) {
-                best_count = int(sel.size());
-                best_sel = sel;
-                std::copy(r, r + kPassBits, best_r);
+            const int count = runnable(c);
+            if (count > best_count || (count == best_count && c < best_c)) {
+                best_count = count;
+                best_c = c;
             }
         }
-        std::vector<TileOp> members;
+        int best_r[kPassBits], ri = 0;
+        for (int i = 0; i < U; i++)
+            if (best_c >> i & 1u) best_r[ri++] = upper[i];
+        std::vector<int> best_sel;
+        {
+            uint64_t blocked = 0;
+            for (size_t i = 0; i < live.size(); i++) {
+                if (!(lneed[i] & ~best_c) && !(lqm[i] & blocked))
+                    best_sel.push_back(live[i]);
+                else
+                    blocked |= lqm[i];
+            }
+        }
         for (int i : best_sel) {
-            members.push_back(pass_member(tops[i], best_r));
+            pass_member(tops[i], best_r);
             done[i] = 1;
             left--;
         }
-        emit_pass(best_r, members, prog);
+        emit_pass(best_r, tops, best_sel, prog);
     }
 }
 

@@ -52,6 +52,15 @@ struct DfAcc {
         add(p);
     }
     __device__ __forceinline__ void sub_prod(float a, float b) { add_prod(-a, b); }
+    // Sum over the warp in lane 0 (fixed shuffle order), still as a float pair.
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float os = __shfl_down_sync(0xffffffffu, s, o), oc = __shfl_down_sync(0xffffffffu, c, o);
+            add(os);
+            c = __fadd_rn(c, oc);
+        }
+    }
 };
 
 }  // namespace qs

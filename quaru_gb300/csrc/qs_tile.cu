@@ -572,15 +572,11 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
                          (sizeof(uint64_t) << sa.RH);
     sa.nbuf = (3 * tile_bytes + fixed <= 110 * 1024) ? 3 : 2;  // three buffers where two blocks still fit an SM
     const size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_tile<REP, BLK>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
-    }
     const uint64_t ntiles = 1ull << (n - st.T);
     // One wave exactly: every CTA walks the same number of tiles, so a grid larger than what is
     // resident would leave a second, partly empty wave.
     int per_sm = 0;
-    cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<REP, BLK>, kTileThreads, smem);
+    cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile<REP, BLK>), kTileThreads, smem, &per_sm);
     if (oe != cudaSuccess) return oe;
     per_sm = std::max(1, per_sm);
     const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * per_sm);
