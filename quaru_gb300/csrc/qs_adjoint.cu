@@ -76,12 +76,43 @@ __global__ void __launch_bounds__(kAT) k_pair_final(const double* __restrict__ p
 struct PauliDev {
     double c;
     uint64_t x, z;
+    float ch, cl;  // c as a float pair, c = ch + cl + O(2^-48 |c|)
+    uint32_t cls;  // |x & z| mod 4: the term's factor i^cls
+    uint32_t pad_;
 };
 
 // out_i = sum_t c_t * i^{|x&z|} * (-1)^{|z & (i^x)|} * psi_{i^x}
-template <typename T>
+template <typename T, bool DFC>
 __global__ void __launch_bounds__(kAT) k_pauli_sum(const T* __restrict__ psi, T* __restrict__ out, uint64_t N,
                                                    const PauliDev* __restrict__ terms, int nt) {
+    static_assert(!DFC || sizeof(T) == 8, "float-pair coefficients serve complex64 states");
+    if constexpr (DFC) {
+        // complex64: each term's product by TwoProduct on the FP32 pipe, summed with TwoSum (DfAcc), the
+        // coefficient's low float folded into the compensation; one rounding to float at the end
+        for (uint64_t i = uint64_t(blockIdx.x) * kAT + threadIdx.x; i < N; i += uint64_t(gridDim.x) * kAT) {
+            DfAcc re, im;
+            for (int t = 0; t < nt; t++) {
+                const PauliDev& p = terms[t];
+                const uint64_t j = i ^ p.x;
+                const float2 v = reinterpret_cast<const float2*>(psi)[j];
+                const bool neg = __popcll(p.z & j) & 1;
+                const float ch = neg ? -p.ch : p.ch, cl = neg ? -p.cl : p.cl;
+                float xr, xi;  // i^cls * v
+                switch (p.cls) {
+                    case 0: xr = v.x; xi = v.y; break;
+                    case 1: xr = -v.y; xi = v.x; break;
+                    case 2: xr = -v.x; xi = -v.y; break;
+                    default: xr = v.y; xi = -v.x; break;
+                }
+                re.add_prod(ch, xr);
+                re.c = __fmaf_rn(cl, xr, re.c);
+                im.add_prod(ch, xi);
+                im.c = __fmaf_rn(cl, xi, im.c);
+            }
+            reinterpret_cast<float2*>(out)[i] = make_float2(__fadd_rn(re.s, re.c), __fadd_rn(im.s, im.c));
+        }
+        return;
+    }
     for (uint64_t i = uint64_t(blockIdx.x) * kAT + threadIdx.x; i < N; i += uint64_t(gridDim.x) * kAT) {
         double re = 0.0, im = 0.0;
         for (int t = 0; t < nt; t++) {
@@ -166,7 +197,8 @@ __global__ void __launch_bounds__(kAT) k_grad_final(const double* __restrict__ p
 // qubits, with which they commute, so every inner product equals the one of the gate-by-gate sweep.
 constexpr int kAdjT = 11;           // tile qubits of the reverse sweep
 constexpr int kAdjThreads = 256;
-constexpr int kAdjMaxRot = 64;      // rotations per stage
+constexpr int kAdjMaxOps = 32;      // gates per stage: the op table is staged in shared memory
+constexpr int kAdjMaxRot = kAdjMaxOps;  // rotations per launch
 
 struct AdjOpDev {
     TileOp t;      // tile-local form (target bit, tuple expansion, controls, matrix of a fixed gate)
@@ -467,15 +499,32 @@ int inner_product(const void* a, int pa, const void* b, int pb, int n, cudaStrea
 
 static std::vector<PauliDev> pauli_table(const qs_pauli_term* terms, size_t nt) {
     std::vector<PauliDev> v(nt);
-    for (size_t t = 0; t < nt; t++) v[t] = {terms[t].coeff, terms[t].x_mask, terms[t].z_mask};
+    for (size_t t = 0; t < nt; t++) {
+        const double c = terms[t].coeff;
+        const float ch = float(c);
+        v[t] = {c, terms[t].x_mask, terms[t].z_mask, ch, float(c - double(ch)),
+                uint32_t(__builtin_popcountll(terms[t].x_mask & terms[t].z_mask) & 3), 0u};
+    }
     return v;
 }
 
+// Whether every coefficient lies where its float pair carries it to FP64 accuracy.
+static bool pauli_df_ok(const std::vector<PauliDev>& ht) {
+    for (const PauliDev& p : ht) {
+        const double a = std::fabs(p.c);
+        if (a != 0.0 && !(a >= 0x1p-90 && a <= 0x1p90)) return false;
+    }
+    return true;
+}
+
 template <typename T>
-static void launch_pauli_sum(const void* psi, void* out, int n, const PauliDev* dterms, int nt, cudaStream_t s,
-                             int sms) {
+static void launch_pauli_sum(const void* psi, void* out, int n, const PauliDev* dterms, int nt, bool df_ok,
+                             cudaStream_t s, int sms) {
     const uint64_t N = 1ull << n;
-    k_pauli_sum<T><<<grid_for_pairs(N, sms), kAT, 0, s>>>((const T*)psi, (T*)out, N, dterms, nt);
+    if (sizeof(T) == 8 && df_ok)
+        k_pauli_sum<float2, true><<<grid_for_pairs(N, sms), kAT, 0, s>>>((const float2*)psi, (float2*)out, N, dterms, nt);
+    else
+        k_pauli_sum<T, false><<<grid_for_pairs(N, sms), kAT, 0, s>>>((const T*)psi, (T*)out, N, dterms, nt);
     note_launches(1);
 }
 
@@ -493,9 +542,10 @@ int expval_pauli(const void* psi, int prec, int n, const qs_pauli_term* terms, s
     if (nt) AJ_CHECK(cudaMemcpyAsync(blob + o_terms, ht.data(), nt * sizeof(PauliDev), cudaMemcpyHostToDevice, s),
                      "terms upload");
     if (prec == QS_PREC_C64)
-        launch_pauli_sum<float2>(psi, blob + o_lam, n, (const PauliDev*)(blob + o_terms), int(nt), s, sms);
+        launch_pauli_sum<float2>(psi, blob + o_lam, n, (const PauliDev*)(blob + o_terms), int(nt), pauli_df_ok(ht),
+                                 s, sms);
     else
-        launch_pauli_sum<double2>(psi, blob + o_lam, n, (const PauliDev*)(blob + o_terms), int(nt), s, sms);
+        launch_pauli_sum<double2>(psi, blob + o_lam, n, (const PauliDev*)(blob + o_terms), int(nt), false, s, sms);
     AJ_CHECK(cudaGetLastError(), "pauli sum");
     if (inner_product(psi, prec, blob + o_lam, prec, n, s, sms, (double*)(blob + o_part), (double*)(blob + o_res)))
         AJ_CHECK(cudaGetLastError(), "inner product");
@@ -545,7 +595,7 @@ static std::vector<double> rotation_matrix(int axis, double c, double s) {
 template <typename T>
 static int adj_grid(int n, int sms) {
     const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 +
-                        size_t(kMaxStageOps) * sizeof(AdjOpDev) + (8u << 6);
+                        size_t(kAdjMaxOps) * sizeof(AdjOpDev) + (8u << 6);
     int per_sm = 1;  // the smaller of the two variants' occupancies (each variant's limit raised to smem)
     resident_blocks(reinterpret_cast<const void*>(k_adj_stage<T, false>), kAdjThreads, smem, &per_sm);
     if (sizeof(T) == 16) {
@@ -579,7 +629,7 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
         }
         src.push_back(int(gg));
     }
-    const std::vector<TileStage> stages = plan_tiles(rops, n, kAdjT, 5, false);
+    const std::vector<TileStage> stages = plan_tiles(rops, n, kAdjT, 5, false, kAdjMaxOps);
     // device tables: every stage's ops (split so a launch holds at most kAdjMaxRot rotations)
     std::vector<AdjOpDev> host;
     struct Launch {
@@ -737,7 +787,8 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
     auto al = [](size_t x) { return ((x + 255) / 256) * 256; };
     const size_t o_cs = 0, o_terms = o_cs + al(cs.size() * 16), o_part = o_terms + al(nt * sizeof(PauliDev) + 1),
                  o_res = o_part + al(size_t(std::max(nrot, 1)) * pgrid * 8 + 4096 * 16),
-                 o_lam = o_res + al((2 + size_t(nrot)) * 8), o_save = o_lam + al(N * amp), total = o_save + N * amp;
+                 o_err = o_res + al((2 + size_t(nrot)) * 8), o_lam = o_err + al(sizeof(int)),
+                 o_save = o_lam + al(N * amp), total = o_save + N * amp;
     unsigned char* blob = nullptr;
     std::vector<double> res(2 + nrot, 0.0);
     int rc = QS_OK;
@@ -752,6 +803,9 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
             AJ_CHECK(cudaMemcpyAsync(blob + o_terms, ht.data(), nt * sizeof(PauliDev), cudaMemcpyHostToDevice, s),
                      "terms upload");
         AJ_CHECK(cudaMemcpyAsync(blob + o_save, state, N * amp, cudaMemcpyDeviceToDevice, s), "save state");
+        int* derr = reinterpret_cast<int*>(blob + o_err);  // raised by a forward tile kernel's bounded wait
+        AJ_CHECK(cudaMemsetAsync(derr, 0, sizeof(int), s), "status flag");
+        int herr = 0;
         // forward
         if (tiled) {
             std::vector<OpDesc> fops(m);
@@ -764,7 +818,8 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
                 }
             }
             const qs_circuit_options fo{1, 5, 0, 0};
-            if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg)) != QS_OK) goto done;
+            // queued without waiting: the reverse sweep is planned while the forward runs
+            if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg, derr)) != QS_OK) goto done;
         }
         for (size_t g = 0; g < m && !tiled; g++) {
             if (rot_slot[g] >= 0) {
@@ -779,9 +834,10 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
         }
         // lambda = H psi, E = Re<psi|lambda>
         if (prec == QS_PREC_C64)
-            launch_pauli_sum<float2>(state, lam, n, (const PauliDev*)(blob + o_terms), int(nt), s, sms);
+            launch_pauli_sum<float2>(state, lam, n, (const PauliDev*)(blob + o_terms), int(nt), pauli_df_ok(ht), s,
+                                     sms);
         else
-            launch_pauli_sum<double2>(state, lam, n, (const PauliDev*)(blob + o_terms), int(nt), s, sms);
+            launch_pauli_sum<double2>(state, lam, n, (const PauliDev*)(blob + o_terms), int(nt), false, s, sms);
         AJ_CHECK(cudaGetLastError(), "pauli sum");
         if (inner_product(state, prec, lam, prec, n, s, sms, part + size_t(std::max(nrot, 1)) * pgrid, dres))
             AJ_CHECK(cudaGetLastError(), "energy");
@@ -815,8 +871,14 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
             AJ_CHECK(cudaGetLastError(), "gradient reduction");
         }
         AJ_CHECK(cudaMemcpyAsync(res.data(), dres, res.size() * 8, cudaMemcpyDeviceToHost, s), "readback");
+        AJ_CHECK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s), "status readback");
         AJ_CHECK(cudaMemcpyAsync(state, blob + o_save, N * amp, cudaMemcpyDeviceToDevice, s), "restore state");
         AJ_CHECK(cudaStreamSynchronize(s), "adjoint sync");
+        if (herr) {
+            *msg = "a tile kernel's bounded wait for its bulk copies gave up";
+            rc = QS_TIMEOUT;
+            goto done;
+        }
         if (energy) *energy = res[0];
         if (grad) {
             for (size_t p = 0; p < np; p++) grad[p] = 0.0;

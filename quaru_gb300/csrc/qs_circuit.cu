@@ -107,7 +107,7 @@ static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* ga
 }
 
 int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops, const qs_gate* gates,
-                const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
+                const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg, int* derr_dev) {
     if (opts.fuse == 2 && gates) return run_blocks(state, n, prec, arith, gates, ops.size(), opts, s, sms, msg);
     if (opts.fuse >= 1) {
         // Tile qubits: 32 KiB of shared memory per tile by default.
@@ -116,7 +116,7 @@ int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDes
         const int L = std::min(5, T);
         std::vector<TileStage> stages =
             plan_tiles(ops, n, T, L, prec == QS_PREC_C128 && arith == QS_ARITH_EXACT);
-        return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg);
+        return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg, nullptr, derr_dev);
     }
     for (size_t g = 0; g < ops.size(); g++) {
         int rc = apply_op(state, n, prec, arith, ops[g], s, sms, msg);

@@ -14,8 +14,8 @@ namespace qs {
 int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStream_t s, int sms, std::string* msg);
 
 // Apply a classified gate list with the fusion strategy in `opts` (gates are
-// the same list, unclassified, for dense-block fusion).
+// the same list, unclassified, for dense-block fusion). derr_dev: see run_tiled.
 int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops, const qs_gate* gates,
-                const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg);
+                const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg, int* derr_dev = nullptr);
 
 }  // namespace qs

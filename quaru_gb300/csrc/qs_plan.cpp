@@ -34,8 +34,10 @@ static uint64_t qubit_mask(const OpDesc& op) {
 
 static bool pure_move(const OpDesc& op) { return op.kind == OP_MONO_PF || op.kind == OP_NOOP; }
 
-std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order) {
+std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order,
+                                  int max_ops) {
     std::vector<TileStage> stages;
+    max_ops = std::max(1, std::min(max_ops, kMaxStageOps));
     if (T > n) T = n;
     if (L > T) L = T;
     const int H = std::min(T - L, kTileMaxHigh);
@@ -63,7 +65,7 @@ std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, 
             uint64_t need = 0;
             for (int j = 0; j < op.k; j++) need |= 1ull << op.tq[j];
             need &= ~low_mask;
-            if (tileable(op) && __builtin_popcountll(high | need) <= H && st.ops.size() < size_t(kMaxStageOps)) {
+            if (tileable(op) && __builtin_popcountll(high | need) <= H && st.ops.size() < size_t(max_ops)) {
                 high |= need;
                 st.ops.push_back(idx);
             } else {

@@ -597,7 +597,7 @@ static bool df64_range_ok(const OpDesc& op) {
 
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
               const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg,
-              const std::vector<float>* block_frags) {
+              const std::vector<float>* block_frags, int* derr_dev) {
     int rep = (prec == QS_PREC_C64) ? 3 : (arith == QS_ARITH_EXACT ? 0 : (arith == QS_ARITH_FMA ? 1 : 2));
     if (rep == 2)
         for (const auto& op : ops)
@@ -623,8 +623,8 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         cudaError_t e = cudaMallocAsync((void**)&dblob, ops_bytes + 256, s);
         if (e != cudaSuccess) return tile_fail(e, "tile op table", msg);
         dops = reinterpret_cast<TileOp*>(dblob);
-        derr = reinterpret_cast<int*>(dblob + ops_bytes);
-        e = cudaMemsetAsync(derr, 0, sizeof(int), s);
+        derr = derr_dev ? derr_dev : reinterpret_cast<int*>(dblob + ops_bytes);
+        if (!derr_dev) e = cudaMemsetAsync(derr, 0, sizeof(int), s);
         if (e == cudaSuccess && !host.empty())
             e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(TileOp), cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) {
@@ -667,7 +667,7 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         }
         if (e != cudaSuccess) rc = tile_fail(e, "tile kernel", msg);
     }
-    if (rc == QS_OK) {  // a bounded wait inside a tile kernel that gave up is reported here
+    if (rc == QS_OK && !derr_dev) {  // a bounded wait inside a tile kernel that gave up is reported here
         int herr = 0;
         cudaError_t e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);

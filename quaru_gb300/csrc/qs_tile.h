@@ -96,8 +96,10 @@ struct TileStage {
 bool tileable(const OpDesc& op);
 
 // Greedy stage planner with reordering of commuting gates (gates that share no
-// qubit). exact_order keeps arithmetic gates in their original relative order.
-std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order);
+// qubit). exact_order keeps arithmetic gates in their original relative order; a stage holds at most
+// max_ops (<= kMaxStageOps) gates.
+std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order,
+                                  int max_ops = kMaxStageOps);
 
 // Device image of one op inside `stage`.
 TileOp make_tile_op(const OpDesc& op, const TileStage& stage);
@@ -117,9 +119,12 @@ bool pass_only(const std::vector<TileOp>& prog);
 cudaError_t launch_pass(void* state, int n, const TileStage& st, int op_begin, int op_end, const TileOp* dops,
                         int* derr, cudaStream_t s, int sms);
 
-// Run stages on the device; ops are the host descriptors.
+// Run stages on the device; ops are the host descriptors. With derr_dev null, waits for the stages and
+// reports a tile kernel's bounded wait that gave up (QS_TIMEOUT); otherwise the kernels raise the
+// caller's device flag *derr_dev (zeroed by the caller) and the call returns once the stages are
+// queued, leaving the wait and the check to the caller.
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
               const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg,
-              const std::vector<float>* block_frags = nullptr);
+              const std::vector<float>* block_frags = nullptr, int* derr_dev = nullptr);
 
 }  // namespace qs

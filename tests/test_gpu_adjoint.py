@@ -60,6 +60,22 @@ def test_expval_pauli_matches_numpy():
     assert abs(reg.expval_pauli(terms) - energy_np(psi, terms)) < 1e-12
 
 
+def test_expval_pauli_complex64_matches_numpy():
+    """complex64 state: H|psi> summed on the FP32 pipe in compensated float pairs and rounded once to
+    float, so <psi|H|psi> is within a few float roundings of lambda of the FP64 value."""
+    import quaru_gb300 as q
+
+    rng = np.random.default_rng(3)
+    n = 11
+    psi = rand_state(rng, n).astype(np.complex64).astype(np.complex128)
+    terms = [(float(rng.normal()), int(rng.integers(1 << n)), int(rng.integers(1 << n))) for _ in range(40)]
+    terms += [(0.7, 0, 0b11), (-1.3, 0b100, 0), (0.25, 0b1000, 0b1000), (1e-3, 0b110, 0b011)]
+    reg = q.Register.from_int(n, 0, precision=1)
+    reg.state = psi
+    bound = 4 * 2.0 ** -24 * sum(abs(c) for c, _, _ in terms)
+    assert abs(reg.expval_pauli(terms) - energy_np(psi, terms)) < bound
+
+
 def energy_gpu(q, n, gates, params, terms, precision=0):
     reg = q.Register.from_int(n, 0, precision=precision)
     reg.set_arith(1)
