@@ -111,24 +111,24 @@ __global__ void __launch_bounds__(kAT) k_pauli_sum(const T* __restrict__ psi, T*
             }
             reinterpret_cast<float2*>(out)[i] = make_float2(__fadd_rn(re.s, re.c), __fadd_rn(im.s, im.c));
         }
-        return;
-    }
-    for (uint64_t i = uint64_t(blockIdx.x) * kAT + threadIdx.x; i < N; i += uint64_t(gridDim.x) * kAT) {
-        double re = 0.0, im = 0.0;
-        for (int t = 0; t < nt; t++) {
-            const PauliDev p = terms[t];
-            const uint64_t j = i ^ p.x;
-            const double2 v = ld2(psi, j);
-            double c = p.c;
-            if (__popcll(p.z & j) & 1) c = -c;
-            switch (__popcll(p.x & p.z) & 3) {
-                case 0: re = fma(c, v.x, re); im = fma(c, v.y, im); break;
-                case 1: re = fma(-c, v.y, re); im = fma(c, v.x, im); break;  // i * v
-                case 2: re = fma(-c, v.x, re); im = fma(-c, v.y, im); break;
-                default: re = fma(c, v.y, re); im = fma(-c, v.x, im); break;  // -i * v
+    } else {
+        for (uint64_t i = uint64_t(blockIdx.x) * kAT + threadIdx.x; i < N; i += uint64_t(gridDim.x) * kAT) {
+            double re = 0.0, im = 0.0;
+            for (int t = 0; t < nt; t++) {
+                const PauliDev p = terms[t];
+                const uint64_t j = i ^ p.x;
+                const double2 v = ld2(psi, j);
+                double c = p.c;
+                if (__popcll(p.z & j) & 1) c = -c;
+                switch (__popcll(p.x & p.z) & 3) {
+                    case 0: re = fma(c, v.x, re); im = fma(c, v.y, im); break;
+                    case 1: re = fma(-c, v.y, re); im = fma(c, v.x, im); break;  // i * v
+                    case 2: re = fma(-c, v.x, re); im = fma(-c, v.y, im); break;
+                    default: re = fma(c, v.y, re); im = fma(-c, v.x, im); break;  // -i * v
+                }
             }
+            st2(out, i, make_double2(re, im));
         }
-        st2(out, i, make_double2(re, im));
     }
 }
 
@@ -205,7 +205,7 @@ struct AdjOpDev {
     int rot;       // stage-local rotation slot, or -1 for a fixed gate
     int axis;      // QS_GATE_RX / RY / RZ
     double c, s;   // cos(theta/2), -sin(theta/2): the inverse rotation
-    int pad_[2];
+    float cf, sf;  // the same rounded to float (complex64 tiles)
 };
 
 static_assert(sizeof(AdjOpDev) % 16 == 0, "the op table is copied to shared memory in 16-byte words");
@@ -227,8 +227,14 @@ __device__ __forceinline__ void adj_fixed(T* s, const TileOp& op, uint32_t tsize
     for (int j = 0; j < 5; j++) seg[j] = op.seg[j];
     if (op.kind == OP_DENSE || op.kind == OP_DENSE_REAL) {
         const uint32_t tb = op.off[1];
-        const R m0 = R(op.m[0]), m1 = R(op.m[1]), m2 = R(op.m[2]), m3 = R(op.m[3]);
-        const R m4 = R(op.m[4]), m5 = R(op.m[5]), m6 = R(op.m[6]), m7 = R(op.m[7]);
+        // complex64 tiles read the host-rounded float copy (no FP64-pipe conversions per thread)
+        const auto* mm = [&] {
+            if constexpr (sizeof(R) == 4)
+                return op.mf;
+            else
+                return op.m;
+        }();
+        const R m0 = mm[0], m1 = mm[1], m2 = mm[2], m3 = mm[3], m4 = mm[4], m5 = mm[5], m6 = mm[6], m7 = mm[7];
         for (uint32_t p = threadIdx.x; p < ntup; p += kAdjThreads) {
             const uint32_t i0 = tuple_index(p, op.npos, seg, op.pos, op.lfixval);
             const T a = s[i0], b = s[i0 | tb];
@@ -253,7 +259,11 @@ __device__ __forceinline__ void adj_fixed(T* s, const TileOp& op, uint32_t tsize
             if (r >= D || op.pf[r] == PF_SKIP_DEV) continue;
             T v = y[r];
             if (op.pf[r] == 255) {
-                const R pr = R(op.m[2 * r]), pi = R(op.m[2 * r + 1]);
+                R pr, pi;
+                if constexpr (sizeof(R) == 4)
+                    pr = op.mf[2 * r], pi = op.mf[2 * r + 1];
+                else
+                    pr = op.m[2 * r], pi = op.m[2 * r + 1];
                 v = cfma(pr, pi, y[r], czero<T>());
             } else {
                 v = apply_pf(y[r], op.pf[r]);
@@ -273,7 +283,11 @@ __device__ __forceinline__ auto adj_rot_tile(T* sp, T* sl, const AdjOpDev& op, u
 #pragma unroll
     for (int j = 0; j < 5; j++) seg[j] = t.seg[j];
     const uint32_t tb = 1u << t.tb[0];
-    const R c = R(op.c), sn = R(op.s);
+    R c, sn;
+    if constexpr (sizeof(R) == 4)
+        c = op.cf, sn = op.sf;
+    else
+        c = op.c, sn = op.s;
     double acc = 0.0;
     DfAcc facc;
     for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += kAdjThreads) {
@@ -663,6 +677,8 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
                 e.axis = gates[g].kind;
                 e.c = std::cos(0.5 * th);
                 e.s = -std::sin(0.5 * th);
+                e.cf = float(e.c);
+                e.sf = float(e.s);
             }
             host.push_back(e);
             cur.count++;
@@ -671,9 +687,13 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
     }
     AdjOpDev* dops = nullptr;
     if (!host.empty()) {
-        cudaError_t e = cudaMallocAsync((void**)&dops, host.size() * sizeof(AdjOpDev), s);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(AdjOpDev), cudaMemcpyHostToDevice, s);
+        const size_t bytes = host.size() * sizeof(AdjOpDev);
+        cudaError_t e = cudaMallocAsync((void**)&dops, bytes, s);
+        if (e == cudaSuccess) {  // page-locked: the upload does not wait for the forward pass queued before it
+            void* stage = pinned_staging(1, bytes);
+            if (stage) std::memcpy(stage, host.data(), bytes);
+            e = cudaMemcpyAsync(dops, stage ? stage : host.data(), bytes, cudaMemcpyHostToDevice, s);
+        }
         if (e != cudaSuccess) return fail(e, "reverse-sweep tables", msg);
     }
     int rc = QS_OK;

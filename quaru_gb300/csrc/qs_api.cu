@@ -5,6 +5,7 @@
 // register owns one device buffer, one CUDA stream and small scratch areas.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -37,6 +38,35 @@ struct qs_register {
 namespace qs {
 static std::atomic<uint64_t> g_launches{0};
 void note_launches(uint64_t count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+
+namespace {
+struct PinnedSlots {
+    void* p[2] = {nullptr, nullptr};
+    size_t cap[2] = {0, 0};
+    ~PinnedSlots() {
+        for (void* q : p)
+            if (q) cudaFreeHost(q);
+    }
+};
+thread_local PinnedSlots t_pinned;
+}  // namespace
+
+void* pinned_staging(int slot, size_t bytes) {
+    if (slot < 0 || slot > 1) return nullptr;
+    if (bytes <= t_pinned.cap[slot]) return t_pinned.p[slot];
+    if (t_pinned.p[slot]) cudaFreeHost(t_pinned.p[slot]);
+    t_pinned.p[slot] = nullptr;
+    t_pinned.cap[slot] = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 2, size_t(1) << 16);
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, want, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    t_pinned.p[slot] = q;
+    t_pinned.cap[slot] = want;
+    return q;
+}
 
 cudaError_t resident_blocks(const void* func, int threads, size_t smem, int* per_sm) {
     static std::mutex mu;

@@ -754,6 +754,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
     if (e == cudaSuccess) e = cudaMallocHost(&b->hcs, 16 * (size_t(b->ncs) + 1));
     if (e == cudaSuccess) e = cudaMallocHost(&b->hres, 8 * (size_t(b->nres) + 1));
     if (e == cudaSuccess) e = cudaMallocHost(&b->herr, sizeof(int));
+    if (e == cudaSuccess) *b->herr = 0;  // page-locked memory comes uninitialised; read even when no run precedes
     b->smem = batch_smem(b->prec);
     if (e == cudaSuccess)
         e = b->prec == QS_PREC_C64

@@ -21,6 +21,12 @@ void note_launches(uint64_t count);
 // two runtime queries once.
 cudaError_t resident_blocks(const void* func, int threads, size_t smem, int* per_sm);
 
+// Page-locked host staging buffer `slot` (0 or 1) of the calling thread, at least `bytes` long, or
+// null if it cannot be had. Uploads from it do not wait for earlier work on the stream (uploads from
+// pageable memory may). A slot is rewritten by the thread's next request for it: callers wait for
+// the stream that reads it before returning, so the next request finds the copy done.
+void* pinned_staging(int slot, size_t bytes);
+
 // Set the message qs_last_error() returns on the calling thread.
 void set_last_error_message(const std::string& msg);
 

@@ -287,6 +287,19 @@ static void pass_member(TileOp& t, const int (&r)[kPassBits]) {
                 if (t.pf[row] != PF_ONE) ones = false;
             }
             code = swapped ? (ones ? PC_SWAP : PC_SWAPPH) : PC_DIAG2;
+            if (code != PC_SWAP && all && nocond && !t.omask) {
+                // uncontrolled phases (RZ, S, T, Y): the 2x2 matrix they are (dest row r takes factor_r
+                // times source row perm[r]) joins the dense groups, which the copy-warp pass kernel runs
+                const double f[4] = {t.m[0], t.m[1], t.m[2], t.m[3]};
+                for (int i = 0; i < 16; i++) t.m[i] = 0.0;
+                const int c0 = swapped ? 1 : 0;  // column of row 0's source
+                t.m[2 * c0] = f[0];
+                t.m[2 * c0 + 1] = f[1];
+                t.m[4 + 2 * (1 - c0)] = f[2];
+                t.m[4 + 2 * (1 - c0) + 1] = f[3];
+                for (int i = 0; i < 8; i++) pm.u[i] = float(t.m[i]);
+                code = PC_DENSE;
+            }
         }
         const int lb = t.tb[0];
         if (lb < kLaneBits) {

@@ -37,15 +37,18 @@ __device__ __forceinline__ double im_term(double2 l0, double2 l1, double2 a, dou
     return (l0.x * a.y - l0.y * a.x) - (l1.x * b.y - l1.y * b.x);
 }
 
+// complex64: the pair's four products summed by an FMA chain (one float rounding per product), the
+// pair sums then accumulated with TwoSum compensation, so the sum over a tile carries no FP32 drift.
 template <int AXIS>
 __device__ __forceinline__ void im_term_acc(DfAcc& acc, float2 l0, float2 l1, float2 a, float2 b) {
-    if (AXIS == QS_GATE_RX) {
-        acc.add_prod(l0.x, b.y); acc.sub_prod(l0.y, b.x); acc.add_prod(l1.x, a.y); acc.sub_prod(l1.y, a.x);
-    } else if (AXIS == QS_GATE_RY) {
-        acc.add_prod(l1.x, a.x); acc.add_prod(l1.y, a.y); acc.sub_prod(l0.x, b.x); acc.sub_prod(l0.y, b.y);
-    } else {
-        acc.add_prod(l0.x, a.y); acc.sub_prod(l0.y, a.x); acc.sub_prod(l1.x, b.y); acc.add_prod(l1.y, b.x);
-    }
+    float t;
+    if (AXIS == QS_GATE_RX)
+        t = __fmaf_rn(l0.x, b.y, __fmaf_rn(-l0.y, b.x, __fmaf_rn(l1.x, a.y, __fmul_rn(-l1.y, a.x))));
+    else if (AXIS == QS_GATE_RY)
+        t = __fmaf_rn(l1.x, a.x, __fmaf_rn(l1.y, a.y, __fmaf_rn(-l0.x, b.x, __fmul_rn(-l0.y, b.y))));
+    else
+        t = __fmaf_rn(l0.x, a.y, __fmaf_rn(-l0.y, a.x, __fmaf_rn(-l1.x, b.y, __fmul_rn(l1.y, b.x))));
+    acc.add(t);
 }
 
 // ---- double-float forms. Amplitudes as float4 (re_hi, re_lo, im_hi, im_lo); each pair's

@@ -625,8 +625,12 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         dops = reinterpret_cast<TileOp*>(dblob);
         derr = derr_dev ? derr_dev : reinterpret_cast<int*>(dblob + ops_bytes);
         if (!derr_dev) e = cudaMemsetAsync(derr, 0, sizeof(int), s);
-        if (e == cudaSuccess && !host.empty())
-            e = cudaMemcpyAsync(dops, host.data(), host.size() * sizeof(TileOp), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !host.empty()) {
+            const size_t bytes = host.size() * sizeof(TileOp);
+            void* stage = pinned_staging(0, bytes);
+            if (stage) std::memcpy(stage, host.data(), bytes);
+            e = cudaMemcpyAsync(dops, stage ? stage : host.data(), bytes, cudaMemcpyHostToDevice, s);
+        }
         if (e != cudaSuccess) {
             cudaFreeAsync(dblob, s);
             return tile_fail(e, "tile op upload", msg);
