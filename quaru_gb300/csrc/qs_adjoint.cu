@@ -622,13 +622,16 @@ static int adj_grid(int n, int sms) {
 }
 
 // The reverse sweep as tiled stages: gates m-1 .. 0, rotations with their inner products, fixed
-// gates as their inverses (inv). Partials of rotation slot r land in part[r * grid .. + grid).
+// gates as their inverses (inv, whose entries are moved out). Partials of rotation slot r land in
+// part[r * grid .. + grid).
 template <typename T>
 static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, const qs_param_gate* gates, size_t m,
-                         const double* params, const std::vector<int>& rot_slot, const std::vector<OpDesc>& inv,
+                         const double* params, const std::vector<int>& rot_slot, std::vector<OpDesc>& inv,
                          double* part, int grid, cudaStream_t s, int sms, std::string* msg) {
     std::vector<OpDesc> rops;
     std::vector<int> src;
+    rops.reserve(m);
+    src.reserve(m);
     for (size_t gg = m; gg-- > 0;) {
         if (rot_slot[gg] >= 0) {  // planning form: a dense 1-qubit gate on the rotation's target
             OpDesc d;
@@ -639,7 +642,7 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
             d.touched_rows = 2;
             rops.push_back(std::move(d));
         } else {
-            rops.push_back(inv[gg]);
+            rops.push_back(std::move(inv[gg]));  // consumed: the caller reads inv no further
         }
         src.push_back(int(gg));
     }
@@ -834,7 +837,7 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
                     const std::vector<double> R = rotation_matrix(gates[g].kind, cs[g].x, cs[g].y);
                     classify_gate(R.data(), 1, gates[g].targets, &fops[g]);
                 } else {
-                    fops[g] = fwd[g];
+                    fops[g] = std::move(fwd[g]);  // the tiled path reads fwd no further
                 }
             }
             const qs_circuit_options fo{1, 5, 0, 0};

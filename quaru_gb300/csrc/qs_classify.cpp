@@ -82,6 +82,25 @@ static inline uint64_t deposit(uint64_t s, uint64_t mask) {
     return r;
 }
 
+// Zero-filled scratch array of n entries: on the stack up to 64 (gates of up to 6 qubits, the
+// common case), on the heap beyond.
+template <typename T>
+struct Scratch {
+    T local[64];
+    std::vector<T> heap;
+    T* p;
+    explicit Scratch(size_t n) {
+        if (n <= 64) {
+            p = local;
+        } else {
+            heap.resize(n);
+            p = heap.data();
+        }
+        std::fill(p, p + n, T());
+    }
+    T& operator[](size_t i) { return p[i]; }
+};
+
 void classify_gate(const double* U, size_t k, const size_t* targets, OpDesc* op) {
     const uint64_t dim = 1ull << k;
     auto at = [&](uint64_t r, uint64_t c) { return U + 2 * (r * dim + c); };
@@ -89,7 +108,7 @@ void classify_gate(const double* U, size_t k, const size_t* targets, OpDesc* op)
     op->orig_k = int(k);
 
     // 1. Rows the gate leaves untouched.
-    std::vector<uint8_t> ident(dim, 0);
+    Scratch<uint8_t> ident(dim);
     for (uint64_t r = 0; r < dim; r++) {
         if (!is_one(at(r, r))) continue;
         bool ok = true;
@@ -122,13 +141,13 @@ void classify_gate(const double* U, size_t k, const size_t* targets, OpDesc* op)
     }
     op->k = kk;
     const uint64_t sdim = 1ull << kk;
-    std::vector<uint64_t> full(sdim);
+    Scratch<uint64_t> full(sdim);
     for (uint64_t s = 0; s < sdim; s++) full[s] = deposit(s, free_local) | (common1 & fixed_local);
 
     // 3. Monomial test on the sub-matrix.
     bool mono = true;
-    std::vector<uint32_t> perm(sdim, 0);
-    std::vector<uint32_t> colcount(sdim, 0);
+    Scratch<uint32_t> perm(sdim);
+    Scratch<uint32_t> colcount(sdim);
     for (uint64_t s = 0; s < sdim && mono; s++) {
         int nz = 0;
         for (uint64_t c = 0; c < sdim; c++) {
@@ -145,7 +164,7 @@ void classify_gate(const double* U, size_t k, const size_t* targets, OpDesc* op)
             if (colcount[c] != 1) mono = false;
 
     if (mono) {
-        op->perm = perm;
+        op->perm.assign(perm.p, perm.p + sdim);
         op->phase.resize(2 * sdim);
         op->pf.resize(sdim);
         bool pf_all = true;
