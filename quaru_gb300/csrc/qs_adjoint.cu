@@ -311,7 +311,7 @@ __device__ __forceinline__ auto adj_rot_tile(T* sp, T* sl, const AdjOpDev& op, u
 }
 
 template <int AXIS>
-__device__ __forceinline__ double adj_rot_tile_df(float4* sp, float4* sl, const AdjOpDev& op, uint32_t tsize) {
+__device__ __forceinline__ DfAcc adj_rot_tile_df(float4* sp, float4* sl, const AdjOpDev& op, uint32_t tsize) {
     const TileOp& t = op.t;
     uint32_t seg[5];
 #pragma unroll
@@ -320,11 +320,11 @@ __device__ __forceinline__ double adj_rot_tile_df(float4* sp, float4* sl, const 
     float ch, cl, sh, sl_;
     df_split(op.c, ch, cl);
     df_split(op.s, sh, sl_);
-    double acc = 0.0;
+    DfAcc acc;
     for (uint32_t p = threadIdx.x; p < (tsize >> 1); p += kAdjThreads) {
         const uint32_t i0 = tuple_index(p, t.npos, seg, t.pos, 0u), i1 = i0 | tb;
         float4 a = sp[i0], b = sp[i1], l0 = sl[i0], l1 = sl[i1];
-        acc += adj_im_df<AXIS>(l0, l1, a, b);
+        adj_im_df_acc<AXIS>(acc, l0, l1, a, b);
         df_rot_pair<AXIS>(ch, cl, sh, sl_, a, b);
         df_rot_pair<AXIS>(ch, cl, sh, sl_, l0, l1);
         sp[i0] = a;
@@ -416,14 +416,16 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_stage(T* __restrict__ psi, 
             if ((base & op.t.omask) != op.t.oval) continue;  // the same for the whole block
             if (op.rot >= 0) {
                 double v;
-                if constexpr (DF) {
+                if constexpr (DF) {  // the warp's float pairs reduced on the FP32 pipe, one FP64 rejoin
+                    DfAcc f;
                     if (op.axis == QS_GATE_RX)
-                        v = adj_rot_tile_df<QS_GATE_RX>(fp, fl, op, tsize);
+                        f = adj_rot_tile_df<QS_GATE_RX>(fp, fl, op, tsize);
                     else if (op.axis == QS_GATE_RY)
-                        v = adj_rot_tile_df<QS_GATE_RY>(fp, fl, op, tsize);
+                        f = adj_rot_tile_df<QS_GATE_RY>(fp, fl, op, tsize);
                     else
-                        v = adj_rot_tile_df<QS_GATE_RZ>(fp, fl, op, tsize);
-                    v = rd_warp_sum(v);
+                        f = adj_rot_tile_df<QS_GATE_RZ>(fp, fl, op, tsize);
+                    f.warp_reduce();
+                    v = __dadd_rn(df_f2d(f.s), df_f2d(f.c));
                 } else if constexpr (sizeof(T) == 8) {
                     // complex64: the warp's compensated float pairs reduced on the FP32 pipe, one
                     // FP64 rejoin per warp

@@ -74,6 +74,9 @@ struct BOp {
 struct BPauli {
     double c;
     unsigned long long x, z;
+    float ch, cl;  // c as a float pair (complex64 circuits)
+    uint32_t cls;  // |x & z| mod 4: the term's factor i^cls
+    uint32_t pad_;
 };
 
 template <typename T>
@@ -124,12 +127,11 @@ __device__ __forceinline__ uint32_t pair_index(uint32_t p, int tb) {
 
 // One gate of a stage on the tile(s) in shared memory. fwd: psi only; reverse: psi and lambda, with
 // a rotation's inner-product term accumulated (before it is un-applied) into acc.
-template <typename T, int AXIS>
-__device__ __forceinline__ double tile_rot(T* sp, T* sl, uint32_t half, int tb, double c, double sn, bool fwd) {
-    using R = decltype(T().x);
-    const R cc = R(c), ss = R(fwd ? sn : -sn);
+template <typename T, int AXIS, typename R = decltype(T().x)>
+__device__ __forceinline__ auto tile_rot(T* sp, T* sl, uint32_t half, int tb, R c, R sn, bool fwd) {
+    const R cc = c, ss = fwd ? sn : -sn;
     double acc = 0.0;
-    DfAcc facc;  // complex64: compensated FP32 products, rounded to FP64 once per thread
+    DfAcc facc;  // complex64: compensated pair sums, reduced over the warp as a float pair
     for (uint32_t p = threadIdx.x; p < half; p += kBT) {
         const uint32_t i0 = pair_index(p, tb), i1 = i0 | (1u << tb);
         T a = sp[i0], b = sp[i1];
@@ -147,23 +149,25 @@ __device__ __forceinline__ double tile_rot(T* sp, T* sl, uint32_t half, int tb, 
         sp[i0] = a;
         sp[i1] = b;
     }
-    if constexpr (sizeof(R) == 4) acc = __dadd_rn(df_f2d(facc.s), df_f2d(facc.c));
-    return acc;
+    if constexpr (sizeof(R) == 4)
+        return facc;
+    else
+        return acc;
 }
 
 template <int AXIS>
-__device__ __forceinline__ double tile_rot_df(float4* sp, float4* sl, uint32_t half, int tb, double c, double sn,
+__device__ __forceinline__ DfAcc tile_rot_df(float4* sp, float4* sl, uint32_t half, int tb, double c, double sn,
                                               bool fwd) {
     float ch, cl, sh, slo;
     df_split(c, ch, cl);
     df_split(fwd ? sn : -sn, sh, slo);
-    double acc = 0.0;
+    DfAcc acc;
     for (uint32_t p = threadIdx.x; p < half; p += kBT) {
         const uint32_t i0 = pair_index(p, tb), i1 = i0 | (1u << tb);
         float4 a = sp[i0], b = sp[i1];
         if (!fwd) {
             float4 l0 = sl[i0], l1 = sl[i1];
-            acc += adj_im_df<AXIS>(l0, l1, a, b);
+            adj_im_df_acc<AXIS>(acc, l0, l1, a, b);
             df_rot_pair<AXIS>(ch, cl, sh, slo, l0, l1);
             sl[i0] = l0;
             sl[i1] = l1;
@@ -212,6 +216,7 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
     double* sacc = reinterpret_cast<double*>(rowoff + 64);  // [kBMaxRot][8 warps]
     __shared__ uint32_t s_item;
     __shared__ int s_seg, s_stop;
+    __shared__ float2 s_csf[kBMaxRot];  // complex64: the stage's rotation (cos, sin) rounded to float
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -253,7 +258,35 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
             const int cl = C.n - 1 - C.nche_log;
             const uint64_t p0 = uint64_t(j) << cl, p1 = p0 + (1ull << cl);
             double e = 0.0;
+            DfAcc eacc;  // complex64: the energy terms as a compensated float pair
             for (uint64_t i = 2 * p0 + threadIdx.x; i < 2 * p1; i += kBT) {
+                if constexpr (sizeof(T) == 8) {  // complex64: products and sums in compensated float pairs
+                    DfAcc fre, fim;
+                    for (int t = 0; t < C.nterms; t++) {
+                        const BPauli& P = terms[C.term_off + t];
+                        const uint64_t k = i ^ P.x;
+                        const float2 v = St<T>::ld(psi, k);
+                        const bool neg = __popcll(P.z & k) & 1;
+                        const float ch = neg ? -P.ch : P.ch, cl = neg ? -P.cl : P.cl;
+                        float xr, xi;  // i^cls * v
+                        switch (P.cls) {
+                            case 0: xr = v.x; xi = v.y; break;
+                            case 1: xr = -v.y; xi = v.x; break;
+                            case 2: xr = -v.x; xi = -v.y; break;
+                            default: xr = v.y; xi = -v.x; break;
+                        }
+                        fre.add_prod(ch, xr);
+                        fre.c = __fmaf_rn(cl, xr, fre.c);
+                        fim.add_prod(ch, xi);
+                        fim.c = __fmaf_rn(cl, xi, fim.c);
+                    }
+                    const float2 lv = make_float2(__fadd_rn(fre.s, fre.c), __fadd_rn(fim.s, fim.c));
+                    St<T>::st(lam, i, lv);
+                    const float2 pv = St<T>::ld(psi, i);  // energy term Re(conj(psi_i) lambda_i)
+                    eacc.add_prod(pv.x, lv.x);
+                    eacc.add_prod(pv.y, lv.y);
+                    continue;
+                }
                 double re = 0.0, im = 0.0;
                 for (int t = 0; t < C.nterms; t++) {
                     const BPauli P = terms[C.term_off + t];
@@ -272,6 +305,7 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
                 const double2 pv = St<T>::d(St<T>::ld(psi, i));
                 e = fma(pv.x, re, fma(pv.y, im, e));
             }
+            if constexpr (sizeof(T) == 8) e = __dadd_rn(df_f2d(eacc.s), df_f2d(eacc.c));
             double dummy = 0.0;
             rd_block_sum2<kBT>(e, dummy);
             if (threadIdx.x == 0) partials[C.epart_off + j] = e;
@@ -289,6 +323,14 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
             }
             if (!fwd)
                 for (int r = threadIdx.x; r < S.nrot * (kBT / 32); r += kBT) sacc[r] = 0.0;
+            if constexpr (sizeof(T) == 8)  // one conversion per rotation per item, not per thread and tile
+                for (int o = threadIdx.x; o < S.nops; o += kBT) {
+                    const BOp op = ops[S.op_off + o];
+                    if (op.kind != kCnot && op.kind != kFix1) {
+                        const double2 t2 = cs[op.cs];
+                        s_csf[o] = make_float2(float(t2.x), float(t2.y));
+                    }
+                }
             __syncthreads();
             float4* fp = reinterpret_cast<float4*>(sp);
             float4* fl = reinterpret_cast<float4*>(sl);
@@ -338,21 +380,36 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
                             tile_fix1(sp, half, op.tb, op.m, !fwd);
                             if (!fwd) tile_fix1(sl, half, op.tb, op.m, true);
                         }
+                    } else if constexpr (sizeof(T) == 8) {  // complex64
+                        const float2 t2 = s_csf[o];
+                        DfAcc f;
+                        if (op.kind == QS_GATE_RX) f = tile_rot<T, QS_GATE_RX>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                        else if (op.kind == QS_GATE_RY) f = tile_rot<T, QS_GATE_RY>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                        else f = tile_rot<T, QS_GATE_RZ>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
+                        if (!fwd) {  // the warp's float pairs reduced on the FP32 pipe, one FP64 rejoin
+                            f.warp_reduce();
+                            if (lane == 0) sacc[op.lrot * (kBT / 32) + warp] += __dadd_rn(df_f2d(f.s), df_f2d(f.c));
+                        }
                     } else {
                         const double2 t2 = cs[op.cs];
                         double v;
                         if (df) {
-                            if (op.kind == QS_GATE_RX) v = tile_rot_df<QS_GATE_RX>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
-                            else if (op.kind == QS_GATE_RY) v = tile_rot_df<QS_GATE_RY>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
-                            else v = tile_rot_df<QS_GATE_RZ>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            DfAcc f;
+                            if (op.kind == QS_GATE_RX) f = tile_rot_df<QS_GATE_RX>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            else if (op.kind == QS_GATE_RY) f = tile_rot_df<QS_GATE_RY>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            else f = tile_rot_df<QS_GATE_RZ>(fp, fl, half, op.tb, t2.x, t2.y, fwd);
+                            v = 0.0;
+                            if (!fwd) {  // float pairs over the warp, one FP64 rejoin
+                                f.warp_reduce();
+                                v = __dadd_rn(df_f2d(f.s), df_f2d(f.c));
+                            }
                         } else {
                             if (op.kind == QS_GATE_RX) v = tile_rot<T, QS_GATE_RX>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
                             else if (op.kind == QS_GATE_RY) v = tile_rot<T, QS_GATE_RY>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
                             else v = tile_rot<T, QS_GATE_RZ>(sp, sl, half, op.tb, t2.x, t2.y, fwd);
                         }
                         if (!fwd) {
-#pragma unroll
-                            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+                            if (!df) v = rd_warp_sum(v);
                             if (lane == 0) sacc[op.lrot * (kBT / 32) + warp] += v;
                         }
                     }
@@ -714,7 +771,10 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
                 release(b);
                 return fail(QS_INVALID_ARGUMENT, "circuit " + std::to_string(c) + ": Pauli term acts on a qubit >= n");
             }
-            terms.push_back({q.terms[t].coeff, q.terms[t].x_mask, q.terms[t].z_mask});
+            const double c = q.terms[t].coeff;
+            const float ch = float(c);
+            terms.push_back({c, q.terms[t].x_mask, q.terms[t].z_mask, ch, float(c - double(ch)),
+                             uint32_t(__builtin_popcountll(q.terms[t].x_mask & q.terms[t].z_mask) & 3), 0u});
         }
         C.nrot = int(rp.size());
         plan_circuit(q, C.T, b->prec == QS_PREC_C128 && b->arith == QS_ARITH_DF64, &C, cs_of, rslot_of, &stages,

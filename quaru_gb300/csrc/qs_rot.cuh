@@ -52,9 +52,10 @@ __device__ __forceinline__ void im_term_acc(DfAcc& acc, float2 l0, float2 l1, fl
 }
 
 // ---- double-float forms. Amplitudes as float4 (re_hi, re_lo, im_hi, im_lo); each pair's
-// Im<lambda|A|psi> is a double-float dot product rounded once to FP64 (df_dot).
+// Im<lambda|A|psi> is a double-float dot product (df_dot_pair), added to a compensated float-pair
+// accumulator: no FP64 operation per pair.
 template <int AXIS>
-__device__ __forceinline__ double adj_im_df(float4 l0, float4 l1, float4 a, float4 b) {
+__device__ __forceinline__ void adj_im_df_acc(DfAcc& acc, float4 l0, float4 l1, float4 a, float4 b) {
     // terms u * x of Im<lambda|A|psi> (see im_term): u from lambda, x from psi
     float uh[4], ul[4], xh[4], xl[4];
     auto set = [&](int k, float vh, float vl, float wh, float wl, bool neg) {
@@ -73,7 +74,10 @@ __device__ __forceinline__ double adj_im_df(float4 l0, float4 l1, float4 a, floa
         set(0, l0.x, l0.y, a.z, a.w, false); set(1, l0.z, l0.w, a.x, a.y, true);
         set(2, l1.x, l1.y, b.z, b.w, true); set(3, l1.z, l1.w, b.x, b.y, false);
     }
-    return df_dot<4>(uh, ul, xh, xl);
+    float h, l;
+    df_dot_pair<4>(uh, ul, xh, xl, h, l);
+    acc.add(h);
+    acc.c = __fadd_rn(acc.c, l);
 }
 
 // c * p + q2 * r in double-float: the rot_pair formulas with (c, s) = (ch + cl, sh + sl).
