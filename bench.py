@@ -419,6 +419,7 @@ def adjoint_section(q, torch, args) -> dict:
     from quaru_gb300.workloads import config4
 
     gates, params, terms = config4()
+    circuit, observable = q.ParamCircuit(gates), q.PauliSum(terms)  # converted once, as an optimiser loop would
     n = 20
     out = {"workload": "20-qubit hardware-efficient ansatz, 10 layers (RY, RZ on every qubit + CNOT ladder), "
                        "400 parameters, H = sum a_i Z_i Z_i+1 + sum b_i X_i"}
@@ -428,11 +429,11 @@ def adjoint_section(q, torch, args) -> dict:
         reg = q.Register.from_int(n, 0, precision=prec)
         reg.set_arith(arith)
         for _ in range(3):
-            e, g = reg.adjoint_gradient(gates, params, terms)
+            e, g = reg.adjoint_gradient(circuit, params, observable)
         reps = 5
         t0 = time.perf_counter()
         for _ in range(reps):
-            e, g = reg.adjoint_gradient(gates, params, terms)
+            e, g = reg.adjoint_gradient(circuit, params, observable)
         dt = (time.perf_counter() - t0) / reps
         grads[name] = g
         out[name] = {"ms_per_gradient": 1e3 * dt, "grads_per_s": len(params) / dt, "energy": e}
@@ -505,7 +506,7 @@ def run_kernels(args) -> None:
     init (basis and product state), dense 1-qubit (exact, FMA, DF64; complex64), CNOT/permutation,
     dense 3-qubit, 6-qubit permutation and dense gates, probability reduction, read-back and
     collapse (both precisions), stages (complex128 DF64 tiles, complex64 register passes, complex64
-    3xTF32 blocks), adjoint, batch."""
+    3xTF32 blocks), adjoint (FP64 and mixed), batch (FP64 and mixed)."""
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
@@ -542,12 +543,14 @@ def run_kernels(args) -> None:
         c.measure(n - 1, 0.5)
         del r, c, p_reg
     gates, params, terms = config4()
-    reg = q.Register.from_int(20, 0)
-    reg.set_arith(q.QS_ARITH_FMA)
-    reg.adjoint_gradient(gates, params, terms)
+    for prec in (q.QS_PREC_C128, q.QS_PREC_C64):  # FP64 and mixed (complex64) adjoint gradients
+        reg = q.Register.from_int(20, 0, precision=prec)
+        reg.set_arith(q.QS_ARITH_FMA)
+        reg.adjoint_gradient(gates, params, terms)
     circuits, bp = config5(count=16, qmin=10, qmax=18, lmin=2, lmax=4, seed=3)
-    b = Batch(circuits, chunk_log2=11, ctas_per_sm=2)
-    b.run(bp)
+    for prec in (q.QS_PREC_C128, q.QS_PREC_C64):
+        b = Batch(circuits, precision=prec, chunk_log2=11, ctas_per_sm=2)
+        b.run(bp)
     print(json.dumps({"kernels": "done", "qubits": n, "launches": int(q._lib.load().qs_launch_count())}))
 
 

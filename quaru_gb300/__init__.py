@@ -7,9 +7,9 @@ Rust API (Register, Operation, the gate constructors) over that ABI.
 from . import _lib
 from ._lib import (QS_ARITH_DF64, QS_ARITH_EXACT, QS_ARITH_FMA, QS_PREC_C64, QS_PREC_C128)
 from .operation import Operation
-from .register import EngineError, OperationError, ParamGate, Register
+from .register import EngineError, OperationError, ParamCircuit, ParamGate, PauliSum, Register
 
-__all__ = ["Register", "ParamGate", "Operation", "OperationError", "EngineError", "QS_PREC_C128", "QS_PREC_C64",
+__all__ = ["Register", "ParamGate", "ParamCircuit", "PauliSum", "Operation", "OperationError", "EngineError", "QS_PREC_C128", "QS_PREC_C64",
            "QS_ARITH_EXACT", "QS_ARITH_FMA", "QS_ARITH_DF64"]
 
 

@@ -284,10 +284,15 @@ class Register:
         return v.value
 
     def adjoint_gradient(self, gates, params, terms):
-        """Energy and gradient of the parameterised circuit `gates` (see ParamGate) for observable `terms`."""
-        table, keep = param_gate_table(gates)
+        """Energy and gradient of the parameterised circuit `gates` (a list of ParamGate, or a
+        ParamCircuit built once from one) for observable `terms` (a list of (coeff, x_mask, z_mask),
+        or a PauliSum)."""
+        if isinstance(gates, ParamCircuit):
+            table, keep = gates.table, None
+        else:
+            table, keep = param_gate_table(gates)
         p = np.ascontiguousarray(np.asarray(params, dtype=np.float64))
-        arr = _pauli_array(terms)
+        arr = terms.array if isinstance(terms, PauliSum) else _pauli_array(terms)
         grad = np.zeros(max(1, p.size), dtype=np.float64)
         e = ctypes.c_double(0)
         err = np.zeros(3, dtype=np.uintp)
@@ -328,6 +333,29 @@ def param_gate_table(gates):
         sizes = np.fromiter((m.size for m in mats), dtype=np.uint64, count=len(mats))
         table["matrix"][fidx] = mflat.ctypes.data + 16 * (np.cumsum(sizes) - sizes)
     return table, (flat, mflat)
+
+
+class ParamCircuit:
+    """A parameterised circuit converted once into the engine's gate records, for repeated gradient
+    calls with new parameters (an optimiser loop): the per-call cost is the engine's alone."""
+
+    def __init__(self, gates):
+        self.gates = list(gates)
+        self.table, self._keep = param_gate_table(self.gates)
+
+    def __len__(self) -> int:
+        return len(self.gates)
+
+
+class PauliSum:
+    """An observable (list of (coeff, x_mask, z_mask)) converted once into the engine's term records."""
+
+    def __init__(self, terms):
+        self.terms = list(terms)
+        self.array = _pauli_array(self.terms)
+
+    def __len__(self) -> int:
+        return len(self.terms)
 
 
 class ParamGate:

@@ -165,6 +165,19 @@ def test_adjoint_tiled_mixed_gates(n, precision, arith):
         assert abs(grad[p] - fd) < tol_fd, (p, grad[p], fd)
 
 
+def test_param_circuit_and_pauli_sum_match_plain_lists():
+    """ParamCircuit / PauliSum (records converted once) give the same energy and gradient as lists."""
+    import quaru_gb300 as q
+    from quaru_gb300.workloads import config4
+
+    gates, params, terms = config4(n=12, layers=3)
+    for precision in (0, 1):
+        reg = q.Register.from_int(12, 0, precision=precision)
+        e1, g1 = reg.adjoint_gradient(gates, params, terms)
+        e2, g2 = reg.adjoint_gradient(q.ParamCircuit(gates), params, q.PauliSum(terms))
+        assert e1 == e2 and np.array_equal(g1, g2)
+
+
 def test_adjoint_config4_size_fp64_and_mixed():
     """20 qubits, 10 layers, 400 parameters: spot-check 6 parameters by parameter shift and central
     differences; the complex64 (mixed) gradient agrees with FP64 to 1e-4 and its state has 1 - F <= 1e-6."""
