@@ -283,6 +283,21 @@ def run_ours(args) -> None:
         fs = f0.elapsed_time(f1) / 1e3
         fused = {"gates_per_s": len(fl) / fs, "ms_per_step": 1e3 * fs / args.steps,
                  "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0)}
+        if prec == q.QS_PREC_C128:
+            # dense fused blocks at the automatic width (double-float arithmetic: 3-qubit blocks)
+            b0 = torch.cuda.Event(enable_timing=True)
+            b1 = torch.cuda.Event(enable_timing=True)
+            reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=2)
+            barrier()
+            l0 = lib.qs_launch_count()
+            b0.record(stream)
+            reg.apply_gates(fl, fuse=2)
+            b1.record(stream)
+            barrier()
+            bs = b0.elapsed_time(b1) / 1e3
+            fused["blocks"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
+                               "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0),
+                               "max_width": 3 if args.arith == "df64" else 2}
         if prec == q.QS_PREC_C64:
             # dense 5-qubit blocks as 3xTF32 tensor-core GEMMs
             b0 = torch.cuda.Event(enable_timing=True)
@@ -298,6 +313,7 @@ def run_ours(args) -> None:
             fused["blocks_tf32x3"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
                                       "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0)}
 
+    widths = None if args.no_widths else width_section(q, torch, args)
     precision = None if args.no_precision else precision_section(q, torch, args)
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
     batch = None if args.no_batch else batch_section(q, args)
@@ -354,6 +370,7 @@ def run_ours(args) -> None:
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
         "clocks": clk,
         "fused": fused,
+        "fusion_widths": widths,
         "precision_form": precision,
         "adjoint": adjoint,
         "batch": batch,
@@ -363,6 +380,45 @@ def run_ours(args) -> None:
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def width_section(q, torch, args) -> dict:
+    """The plain form at scale: a 28-qubit complex128 layered circuit (Haar on every qubit + a CNOT
+    matching per layer) with fusion off (one sweep per gate), cache-blocked stages, and dense fused
+    blocks of width 2..5 (each block one sweep). Per variant: ms, gates/s, sweeps, and the HBM GB/s
+    those sweeps move (each gate's own bytes unfused, 2 * 2^n * 16 bytes per fused sweep).
+    Double-float arithmetic; blocks of 4 and 5 qubits run in FP64 (the double-float kernel covers up
+    to 3). Layers: 40 for the per-gate, stage and 2- and 3-qubit block runs, 10 for the FP64 4- and
+    5-qubit blocks."""
+    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+
+    n = 28
+    lib = q._lib.load()
+    reg = q.Register.from_int(n, 0)
+    reg.set_arith(q.QS_ARITH_DF64)
+    stream = torch.cuda.ExternalStream(reg.stream)
+    sweep_bytes = 2.0 * (1 << n) * 16
+    out = {"workload": f"{n}-qubit layered random circuit, complex128, double-float arithmetic", "qubits": n}
+    variants = [("unfused", 0, 5, 40), ("stages", 1, 5, 40), ("blocks_w2", 2, 2, 40), ("blocks_w3", 2, 3, 40),
+                ("blocks_w4", 2, 4, 10), ("blocks_w5", 2, 5, 10)]
+    for name, fuse, width, layers in variants:
+        ops = flatten(layered_circuit(n, layers, seed_for(2)))
+        reg.apply_gates(ops[: 3 * (n + n // 2)], fuse=fuse, max_width=width)  # warm-up: 3 layers
+        reg.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        l0 = lib.qs_launch_count()
+        a.record(stream)
+        reg.apply_gates(ops, fuse=fuse, max_width=width)
+        b.record(stream)
+        reg.synchronize()
+        s = a.elapsed_time(b) / 1e3
+        sweeps = int(lib.qs_launch_count() - l0)
+        # bytes the sweeps move: per gate (a CNOT touches half the state) unfused, whole states otherwise
+        moved = sum(gate_bytes(g, n, 16) for g in ops) if fuse == 0 else sweeps * sweep_bytes
+        out[name] = {"layers": layers, "gates": len(ops), "ms": 1e3 * s, "gates_per_s": len(ops) / s,
+                     "sweeps": sweeps, "hbm_gbs": moved / s / 1e9}
+    return out
 
 
 def precision_section(q, torch, args) -> dict:
@@ -571,6 +627,7 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
     ap.add_argument("--no-precision", action="store_true", help="skip the 40-layer precision-form section")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-gradient section")
+    ap.add_argument("--no-widths", action="store_true", help="skip the 28-qubit fusion-width section")
     ap.add_argument("--kernels", action="store_true", help="run the per-kernel profiling workload instead")
     args = ap.parse_args()
     if args.warmup < 3:

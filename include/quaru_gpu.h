@@ -115,7 +115,9 @@ typedef struct qs_circuit_options {
     int fuse;        /* 0: one sweep per gate; 1: cache-blocked stages (bit-identical to 0
                         under QS_ARITH_EXACT); 2: dense fused blocks (complex64 registers:
                         3xTF32 tensor-core blocks) */
-    int max_width;   /* widest fused dense block, 2..5 (fuse == 2) */
+    int max_width;   /* widest fused dense block, 2..5 (fuse == 2); 0 = automatic: 5 on complex64
+                        registers (tensor-core blocks), 3 on complex128 with QS_ARITH_DF64 (the
+                        widest double-float dense kernel), 2 otherwise (FP64 blocks) */
     int tile_qubits; /* qubits per shared-memory tile for fuse >= 1; 0 = automatic */
     int reserved;
 } qs_circuit_options;

@@ -70,9 +70,15 @@ int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStre
 // 12-qubit tiles; otherwise each block is one dense gate sweep.
 static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* gates, size_t m,
                       const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
-    const int W = std::max(2, std::min(5, opts.max_width > 0 ? opts.max_width : 5));
-    std::vector<FusedBlock> blocks = fuse_blocks(gates, m, W);
     const bool tensor = (prec == QS_PREC_C64) && n >= 12;
+    // automatic width: where each block's sweep stays cheap. Complex64 blocks are tensor-core GEMMs
+    // at any width up to 5; complex128 double-float blocks run the double-float dense kernel up to 3
+    // qubits (4- and 5-qubit blocks fall back to FP64, which GB300 runs at 1/64 of the FP32 rate);
+    // FP64 blocks cost as many FP64 operations per amplitude as the gates they fuse, so 2 only halves
+    // the sweeps.
+    const int autow = tensor ? 5 : (prec == QS_PREC_C128 && arith == QS_ARITH_DF64) ? 3 : 2;
+    const int W = std::max(2, std::min(5, opts.max_width > 0 ? opts.max_width : autow));
+    std::vector<FusedBlock> blocks = fuse_blocks(gates, m, W);
     std::vector<OpDesc> ops;
     std::vector<float> frags;
     for (FusedBlock& b : blocks) {

@@ -171,7 +171,7 @@ class Register:
         except OperationError as e:
             raise RuntimeError("Could not apply operation") from e
 
-    def apply_gates(self, ops: Iterable[Operation], fuse: int = 0, max_width: int = 5, tile_qubits: int = 0):
+    def apply_gates(self, ops: Iterable[Operation], fuse: int = 0, max_width: int = 0, tile_qubits: int = 0):
         """The operations loop of apply_circuit (src/register.rs:346-350) in one library call."""
         ops = list(ops)
         keep = []

@@ -184,3 +184,21 @@ def test_dense_block_fusion_c128_and_small_registers():
         g.set_arith(1)
         g.apply_gates(ops, fuse=2)
         assert floored_rel_err(g.state, o.state) <= tol, (n, prec)
+
+
+@pytest.mark.parametrize("n", [12, 15])
+def test_dense_block_fusion_c128_double_float(n):
+    """fuse=2 on complex128 with double-float arithmetic: blocks of width 2 and 3 (the automatic width)
+    through the double-float dense kernels, 4 through FP64; all within 1e-12 of the oracle."""
+    import quaru_gb300 as q
+    from oracle.oracle import OracleRegister
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    ops = flatten(layered_circuit(n, 6, 600 + n)) + mixed_circuit(np.random.default_rng(n + 9), n, 80)
+    o = OracleRegister.from_int(n, 0)
+    o.apply_sequence([(g.matrix, g.targets) for g in ops])
+    for w in (0, 2, 3, 4):
+        g = q.Register.from_int(n, 0)
+        g.set_arith(2)
+        g.apply_gates(ops, fuse=2, max_width=w)
+        assert floored_rel_err(g.state, o.state) <= 1e-12, w
