@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kAT) k_grad_final(const double* __restrict__ p
 // tile's pairs to its slot (FP64, per warp, in shared memory) and is un-applied from both tiles; a
 // fixed gate (its inverse) is applied to both. Gates were reordered only past gates on disjoint
 // qubits, with which they commute, so every inner product equals the one of the gate-by-gate sweep.
-constexpr int kAdjT = 11;           // tile qubits of the reverse sweep
+constexpr int kAdjT = 11;           // tile qubits of the reverse sweep (largest; see adj_tile_qubits)
 constexpr int kAdjThreads = 256;
 constexpr int kAdjMaxOps = 32;      // gates per stage: the op table is staged in shared memory
 constexpr int kAdjMaxRot = kAdjMaxOps;  // rotations per launch
@@ -607,9 +607,17 @@ static std::vector<double> rotation_matrix(int axis, double c, double s) {
     return {c, -s, 0, 0, 0, 0, c, s};
 }
 
-// Grid of the tiled reverse sweep for n qubits (the same for every stage, so partials line up).
+// Tile qubits for an n-qubit state: `cap` for large states, fewer below n = cap + 7 so that 128
+// tiles (blocks) share the work of mid-size states, never fewer than 8 (16 tiles at 12 qubits),
+// and the whole state in one tile up to 8 qubits (one block runs every gate without a launch each).
+static int adj_tile_qubits(int n, int cap) { return std::min(n, std::max(8, std::min(cap, n - 7))); }
+
+constexpr int kAdjTiledMin = 6;  // from this many qubits the gradient runs as tiled stages
+
+// Grid of the tiled reverse sweep for n qubits in tiles of tq qubits (the same for every stage, so
+// partials line up).
 template <typename T>
-static int adj_grid(int n, int sms) {
+static int adj_grid(int n, int tq, int sms) {
     const size_t smem = 2 * (sizeof(T) << kAdjT) + size_t(kAdjMaxRot) * (kAdjThreads / 32) * 8 +
                         size_t(kAdjMaxOps) * sizeof(AdjOpDev) + (8u << 6);
     int per_sm = 1;  // the smaller of the two variants' occupancies (each variant's limit raised to smem)
@@ -619,7 +627,7 @@ static int adj_grid(int n, int sms) {
         resident_blocks(reinterpret_cast<const void*>(k_adj_stage<T, sizeof(T) == 16>), kAdjThreads, smem, &df);
         per_sm = std::min(per_sm, df);
     }
-    const uint64_t ntiles = 1ull << (n - kAdjT);
+    const uint64_t ntiles = 1ull << (n - tq);
     return int(std::min<uint64_t>(ntiles, uint64_t(sms) * uint64_t(std::max(1, per_sm))));
 }
 
@@ -648,7 +656,8 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
         }
         src.push_back(int(gg));
     }
-    const std::vector<TileStage> stages = plan_tiles(rops, n, kAdjT, 5, false, kAdjMaxOps);
+    const int tq = adj_tile_qubits(n, kAdjT);
+    const std::vector<TileStage> stages = plan_tiles(rops, n, tq, 5, false, kAdjMaxOps);
     // device tables: every stage's ops (split so a launch holds at most kAdjMaxRot rotations)
     std::vector<AdjOpDev> host;
     struct Launch {
@@ -702,7 +711,7 @@ static int reverse_tiled(void* state, void* lam, int n, int prec, int arith, con
         if (e != cudaSuccess) return fail(e, "reverse-sweep tables", msg);
     }
     int rc = QS_OK;
-    const uint64_t ntiles = 1ull << (n - kAdjT);
+    const uint64_t ntiles = 1ull << (n - tq);
     for (const Launch& L : launches) {
         const TileStage& st = stages[L.stage];
         if (L.first < 0) {  // a gate no tile holds: its inverse on psi and lambda, one sweep each
@@ -806,8 +815,9 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
     std::vector<PauliDev> ht = pauli_table(terms, nt);
     const size_t amp = prec == QS_PREC_C64 ? 8 : 16;
     const uint64_t N = 1ull << n;
-    const bool tiled = n >= kAdjT;  // forward as fused stages, reverse sweep as tiled stages
-    const int pgrid = tiled ? (prec == QS_PREC_C64 ? adj_grid<float2>(n, sms) : adj_grid<double2>(n, sms))
+    const bool tiled = n >= kAdjTiledMin;  // forward as fused stages, reverse sweep as tiled stages
+    const int tq = adj_tile_qubits(n, kAdjT);
+    const int pgrid = tiled ? (prec == QS_PREC_C64 ? adj_grid<float2>(n, tq, sms) : adj_grid<double2>(n, tq, sms))
                             : grid_for_pairs(N >> 1, sms);
     auto al = [](size_t x) { return ((x + 255) / 256) * 256; };
     const size_t o_cs = 0, o_terms = o_cs + al(cs.size() * 16), o_part = o_terms + al(nt * sizeof(PauliDev) + 1),
@@ -842,7 +852,9 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
                     fops[g] = std::move(fwd[g]);  // the tiled path reads fwd no further
                 }
             }
-            const qs_circuit_options fo{1, 5, 0, 0};
+            // tiles as in the reverse sweep: below 18 (complex128) or 19 (complex64) qubits smaller than
+            // the default so that smaller states still spread over many blocks
+            const qs_circuit_options fo{1, 5, adj_tile_qubits(n, prec == QS_PREC_C64 ? 12 : 11), 0};
             // queued without waiting: the reverse sweep is planned while the forward runs
             if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg, derr)) != QS_OK) goto done;
         }
