@@ -116,8 +116,14 @@ int run_circuit(void* state, int n, int prec, int arith, const std::vector<OpDes
                 const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg, int* derr_dev) {
     if (opts.fuse == 2 && gates) return run_blocks(state, n, prec, arith, gates, ops.size(), opts, s, sms, msg);
     if (opts.fuse >= 1) {
-        // Tile qubits: 32 KiB of shared memory per tile by default.
-        int T = opts.tile_qubits > 0 ? opts.tile_qubits : (prec == QS_PREC_C64 ? 12 : 11);
+        // Tile qubits: 32 KiB of shared memory per tile by default; below 19 (complex64) or 18
+        // (complex128) qubits smaller tiles, so that up to 128 blocks share the state (complex64
+        // keeps the 9 tile qubits its register passes need).
+        int T = opts.tile_qubits;
+        if (T <= 0) {
+            const int cap = prec == QS_PREC_C64 ? 12 : 11, floor = prec == QS_PREC_C64 ? 9 : 8;
+            T = std::max(floor, std::min(cap, n - 7));
+        }
         T = std::min(T, n);
         const int L = std::min(5, T);
         std::vector<TileStage> stages =
