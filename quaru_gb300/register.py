@@ -174,18 +174,12 @@ class Register:
     def apply_gates(self, ops: Iterable[Operation], fuse: int = 0, max_width: int = 0, tile_qubits: int = 0):
         """The operations loop of apply_circuit (src/register.rs:346-350) in one library call."""
         ops = list(ops)
-        keep = []
-        gates = (_lib.QsGate * max(1, len(ops)))()
-        for i, op in enumerate(ops):
-            m = _matrix(op.matrix)
-            t = np.ascontiguousarray(np.array(list(op.targets), dtype=np.uintp))
-            keep += [m, t]
-            gates[i].k = len(t)
-            gates[i].targets = _sp(t)
-            gates[i].matrix = _dp(m.view(np.float64))
+        table, keep = gate_table(ops)
         opts = _lib.QsCircuitOptions(fuse, max_width, tile_qubits, 0)
         err = np.zeros(3, dtype=np.uintp)
-        rc = _lib.load().qs_apply_circuit(self._h, gates, len(ops), ctypes.byref(opts), _sp(err))
+        rc = _lib.load().qs_apply_circuit(self._h, table.ctypes.data_as(ctypes.POINTER(_lib.QsGate)), len(ops),
+                                          ctypes.byref(opts), _sp(err))
+        del keep
         _check(rc, err)
         return self
 
@@ -301,6 +295,39 @@ class Register:
                                                _dp(grad), _sp(err)), err)
         del keep
         return e.value, grad[: p.size]
+
+
+_GATE_DTYPE = np.dtype([("k", "<u8"), ("targets", "<u8"), ("matrix", "<u8")])  # qs_gate (include/quaru_gpu.h)
+
+
+def gate_table(ops):
+    """qs_gate records for `ops` as one numpy array, targets and matrices in two shared buffers
+    addressed by offset (a few array operations per call instead of ctypes objects per gate).
+    Raises InvalidDimensions(rows, cols) for a matrix that is not 2^k x 2^k, which the engine could
+    not detect from the record. Returns (table, buffers to keep alive while the table is in use)."""
+    import itertools
+
+    n = len(ops)
+    tl = [op.targets for op in ops]
+    ks = np.fromiter((len(t) for t in tl), dtype=np.uint64, count=n)
+    flat = np.fromiter(itertools.chain.from_iterable(tl), dtype=np.uintp, count=int(ks.sum()) if n else 0)
+    if flat.size == 0:
+        flat = np.zeros(1, dtype=np.uintp)
+    mats = [np.asarray(op.matrix, dtype=np.complex128) for op in ops]
+    for m, k in zip(mats, ks.tolist()):
+        d = 1 << k
+        if m.shape != (d, d):
+            rows = m.shape[0] if m.ndim >= 1 else 0
+            raise OperationError(_lib.QS_INVALID_DIMENSIONS, (rows, m.shape[1] if m.ndim == 2 else 1),
+                                 f"for {k} targets")
+    mflat = np.concatenate([m.reshape(-1) for m in mats]) if mats else np.zeros(1, dtype=np.complex128)
+    table = np.zeros(max(1, n), dtype=_GATE_DTYPE)
+    if n:
+        sizes = np.left_shift(np.uint64(1), 2 * ks)
+        table["k"][:n] = ks
+        table["targets"][:n] = flat.ctypes.data + 8 * (np.cumsum(ks) - ks)
+        table["matrix"][:n] = mflat.ctypes.data + 16 * (np.cumsum(sizes) - sizes)
+    return table, (flat, mflat)
 
 
 _PARAM_GATE_DTYPE = np.dtype([("kind", "<i4"), ("param", "<i4"), ("k", "<u8"), ("targets", "<u8"),

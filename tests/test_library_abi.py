@@ -65,3 +65,30 @@ def test_no_cpu_fallback_without_gpu(lib):
     rc = lib.qs_register_from_int(4, 0, 0, ctypes.byref(h))
     assert rc in (6, 7)  # QS_CUDA_ERROR / QS_OUT_OF_MEMORY: the engine refuses to run without a GPU
     assert not h.value
+
+
+def test_gate_table_records_point_at_each_gate():
+    """The qs_gate records Register.apply_gates builds (one numpy array, shared target and matrix
+    buffers) hold each gate's arity, targets and row-major matrix; a matrix of the wrong shape is
+    InvalidDimensions before anything reaches the engine."""
+    import numpy as np
+
+    from quaru_gb300 import _lib
+    from quaru_gb300 import operation as O
+    from quaru_gb300.operation import Operation
+    from quaru_gb300.register import OperationError, gate_table
+
+    assert ctypes.sizeof(_lib.QsGate) == 24
+    rng = np.random.default_rng(4)
+    ops = [O.hadamard(3), O.cnot(0, 5), O.cnx([1, 2], 4),
+           Operation(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)), [7, 1, 6])]
+    table, keep = gate_table(ops)
+    for rec, op in zip(table, ops):
+        k = int(rec["k"])
+        t = np.frombuffer((ctypes.c_size_t * k).from_address(int(rec["targets"])), dtype=np.uintp)
+        m = np.frombuffer((ctypes.c_double * (2 * 4 ** k)).from_address(int(rec["matrix"])), dtype=np.float64)
+        assert list(t) == list(op.targets)
+        assert np.array_equal(m.view(np.complex128).reshape(1 << k, 1 << k), np.asarray(op.matrix))
+    with pytest.raises(OperationError) as e:
+        gate_table([O.hadamard(0), Operation(np.eye(2), [0, 1])])
+    assert e.value.kind == "InvalidDimensions" and e.value.payload == (2, 2)
