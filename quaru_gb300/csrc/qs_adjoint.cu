@@ -844,19 +844,36 @@ int adjoint_gradient(void* state, int n, int prec, int arith, const qs_param_gat
         // forward
         if (tiled) {
             std::vector<OpDesc> fops(m);
+            std::vector<double> rmat(8 * m);  // the rotations' matrices, in gate order
             for (size_t g = 0; g < m; g++) {
                 if (rot_slot[g] >= 0) {
                     const std::vector<double> R = rotation_matrix(gates[g].kind, cs[g].x, cs[g].y);
+                    std::copy(R.begin(), R.end(), rmat.begin() + 8 * g);
                     classify_gate(R.data(), 1, gates[g].targets, &fops[g]);
                 } else {
                     fops[g] = std::move(fwd[g]);  // the tiled path reads fwd no further
                 }
             }
-            // tiles as in the reverse sweep: below 18 (complex128) or 19 (complex64) qubits smaller than
-            // the default so that smaller states still spread over many blocks
-            const qs_circuit_options fo{1, 5, adj_tile_qubits(n, prec == QS_PREC_C64 ? 12 : 11), 0};
-            // queued without waiting: the reverse sweep is planned while the forward runs
-            if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg, derr)) != QS_OK) goto done;
+            if (prec == QS_PREC_C128 && arith == QS_ARITH_DF64 && n >= 18) {
+                // double-float dense blocks (3 qubits, the automatic width): the fastest complex128
+                // double-float form of a circuit of 1-qubit rotations and CNOTs at 11-qubit tiles (1.85x
+                // the stages at 20 qubits; below 18 qubits the smaller stage tiles win); the blocks are
+                // products of the gates' FP64 matrices
+                std::vector<qs_gate> qg(m);
+                for (size_t g = 0; g < m; g++)
+                    qg[g] = rot_slot[g] >= 0 ? qs_gate{1, gates[g].targets, rmat.data() + 8 * g}
+                                             : qs_gate{gates[g].k, gates[g].targets, gates[g].matrix};
+                const qs_circuit_options fo{2, 0, 0, 0};
+                if ((rc = run_circuit(state, n, prec, arith, fops, qg.data(), fo, s, sms, msg, derr)) != QS_OK)
+                    goto done;
+            } else {
+                // tiles as in the reverse sweep: below 18 (complex128) or 19 (complex64) qubits smaller
+                // than the default so that smaller states still spread over many blocks
+                const qs_circuit_options fo{1, 5, adj_tile_qubits(n, prec == QS_PREC_C64 ? 12 : 11), 0};
+                // queued without waiting: the reverse sweep is planned while the forward runs
+                if ((rc = run_circuit(state, n, prec, arith, fops, nullptr, fo, s, sms, msg, derr)) != QS_OK)
+                    goto done;
+            }
         }
         for (size_t g = 0; g < m && !tiled; g++) {
             if (rot_slot[g] >= 0) {

@@ -116,10 +116,11 @@ def test_adjoint_matches_finite_differences_and_shift(n, layers):
 
 
 @pytest.mark.parametrize("n,precision,arith", [(7, 0, 1), (8, 1, 1), (9, 0, 2), (11, 0, 1), (13, 0, 1), (12, 1, 1),
-                                               (12, 0, 2), (14, 0, 2), (17, 1, 1)])
+                                               (12, 0, 2), (14, 0, 2), (17, 1, 1), (18, 0, 2)])
 def test_adjoint_tiled_mixed_gates(n, precision, arith):
     """n >= 6: forward as fused stages and the reverse sweep as tiled stages (one tile holding the whole
-    state up to 8 qubits, 8-qubit tiles at 11-15, 10 at 17). RX/RY/RZ mixed with
+    state up to 8 qubits, 8-qubit tiles at 11-15, 10 at 17; at 18 qubits the double-float forward
+    runs as 3-qubit dense blocks). RX/RY/RZ mixed with
     fixed gates of every kind the tiles hold (H, S, CZ, CNOT, Toffoli, controlled rotation) and one
     they do not (a dense 2-qubit unitary: its own sweeps), one parameter shared by three rotations;
     every parameter against central differences, and against parameter shift where that is exact.
