@@ -170,13 +170,19 @@ def run_reference(args) -> None:
             total_bytes += gate_bytes(g, n, 16)
             total_t += dt
     value = total_bytes / total_t / 1e9
-    sample = (f"{n}-qubit instance of the layered family, one gate per step (Haar 1q or CNOT), "
-              f"oracle/ C restatement of Register::try_apply_fast (clone + per-tuple gather/mat-vec/scatter)")
+    sample = (f"{n}-qubit instance of the layered family (the {args.qubits}-qubit state and its per-gate clone "
+              f"would need {2 * (16 << args.qubits) / 2**30:.0f} GiB of host memory; GB/s per sweep does not depend "
+              f"on the size once the state exceeds the caches), one gate per step (Haar 1q or CNOT), oracle/ C "
+              f"restatement of Register::try_apply_fast (clone + per-tuple gather/mat-vec/scatter), 1 thread as "
+              f"in the reference")
+    nw = args.qubits
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"layered random circuit, {n} qubits (host), complex128", "qubits": n},
+        "config": {"workload": f"{nw}-qubit layered random circuit (per layer: Haar 1q on all {nw} qubits + "
+                               f"{nw // 2} CNOTs on a random perfect matching), one layer per step",
+                   "qubits": nw, "precision": "c128", "sample_qubits": n, "parallelism": "single (host)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
