@@ -311,6 +311,13 @@ uint64_t qs_launch_count(void);
 /* Library version string. */
 const char* qs_version(void);
 
+/* Failure-detection self-test (no counterpart in the reference): runs the engine's two bounded
+ * device waits, the mbarrier wait of the tile kernels and the completion-counter wait of the
+ * batched kernel, on conditions nothing satisfies, with a ~0.1 s limit. Each wait gives up and
+ * the out-parameters report 1 (timed out); the context stays usable, which the caller can check
+ * with any later call. */
+int qs_selftest_bounded_waits(int* mbar_timed_out, int* counter_timed_out);
+
 #ifdef __cplusplus
 }
 #endif

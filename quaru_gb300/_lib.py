@@ -112,6 +112,7 @@ SIGNATURES = {
     "qs_last_error": (ctypes.c_char_p, []),
     "qs_launch_count": (ctypes.c_uint64, []),
     "qs_version": (ctypes.c_char_p, []),
+    "qs_selftest_bounded_waits": (_i, [_P(_i), _P(_i)]),
 }
 
 _lib: ctypes.CDLL | None = None

@@ -33,6 +33,7 @@
 #include "qs_reduce.cuh"
 #include "qs_rot.cuh"
 #include "qs_tile.h"
+#include "qs_tma.cuh"
 
 namespace qs {
 namespace {
@@ -238,15 +239,9 @@ __global__ void __launch_bounds__(kBT) k_batch(const BCirc* __restrict__ circs, 
         const uint32_t j = s_item - seg_first[s_seg];
         const BCirc C = circs[c];
         if (s > 0 && threadIdx.x == 0) {  // every chunk of the previous step must be done
-            volatile unsigned int* prev = counters + C.counter_off + s - 1;
-            const long long t0 = clock64();
-            while (*prev < unsigned(prevnch)) {
-                __nanosleep(100);
-                if (clock64() - t0 > kWaitCycles) {
-                    atomicExch(err, 1);
-                    s_stop = 1;
-                    break;
-                }
+            if (!counter_wait_bounded(counters + C.counter_off + s - 1, unsigned(prevnch), kWaitCycles)) {
+                atomicExch(err, 1);
+                s_stop = 1;
             }
             __threadfence();
         }

@@ -26,11 +26,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Wait for the phase of `parity` to complete, at most ~2 s of SM clocks.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Wait for the phase of `parity` to complete, at most `limit` SM clocks (default ~2 s); false if the
+// wait gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit = 4000000000LL) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > 4000000000LL) return false;
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+
+// Wait until the counter another block increments reaches `target`, at most `limit` SM clocks;
+// false if the wait gave up.
+__device__ __forceinline__ bool counter_wait_bounded(const volatile unsigned int* c, unsigned int target,
+                                                     long long limit) {
+    const long long t0 = clock64();
+    while (*c < target) {
+        __nanosleep(100);
+        if (clock64() - t0 > limit) return false;
+    }
     return true;
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
