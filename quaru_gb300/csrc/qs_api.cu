@@ -176,6 +176,7 @@ const char* qs_last_error(void) { return g_last_error.c_str(); }
 const char* qs_version(void) { return "quaru-gb300 0.1 (sm_103a)"; }
 
 int qs_register_from_int(size_t n, size_t k, int precision, qs_register** out) {
+    qs::TraceRange trace("qs_register_from_int");
     if (n < 64 && k >= (size_t(1) << n)) return set_err(QS_INVALID_ARGUMENT, "basis index out of range");
     int rc = allocate(n, precision, out);
     if (rc) return rc;
@@ -189,6 +190,7 @@ int qs_register_from_int(size_t n, size_t k, int precision, qs_register** out) {
 }
 
 int qs_register_new(const uint8_t* bits, size_t n, int precision, qs_register** out) {
+    qs::TraceRange trace("qs_register_new");
     if (n > 0 && !bits) return set_err(QS_INVALID_ARGUMENT, "bits is null");
     if (n > kMaxQubits) return set_err(QS_INVALID_ARGUMENT, "too many qubits for one GPU");
     // kron of |0>/|1> vectors (src/register.rs:47-50) is the basis state sum(bits[i] << i).
@@ -200,6 +202,7 @@ int qs_register_new(const uint8_t* bits, size_t n, int precision, qs_register** 
 
 int qs_register_try_from_qubits(const double* qubits, size_t n, int precision, qs_register** out,
                                 size_t* err) {
+    qs::TraceRange trace("qs_register_try_from_qubits");
     if (!out) return set_err(QS_INVALID_ARGUMENT, "output pointer is null");
     *out = nullptr;
     if (n > 0 && !qubits) return set_err(QS_INVALID_ARGUMENT, "qubits is null");
@@ -227,6 +230,7 @@ int qs_register_try_from_qubits(const double* qubits, size_t n, int precision, q
 }
 
 int qs_register_clone(const qs_register* src, qs_register** out) {
+    qs::TraceRange trace("qs_register_clone");
     if (!src) return set_err(QS_INVALID_ARGUMENT, "register is null");
     int rc = allocate(size_t(src->n), src->prec, out);
     if (rc) return rc;
@@ -259,6 +263,7 @@ int qs_register_set_arith(qs_register* reg, int arith) {
 
 int qs_try_apply_fast(qs_register* reg, const double* matrix, size_t rows, size_t cols, const size_t* targets,
                       size_t k, size_t* err) {
+    qs::TraceRange trace("qs_try_apply_fast");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     std::string msg;
     int rc = qs::validate_gate(size_t(reg->n), rows, cols, targets, k, err, &msg);
@@ -271,6 +276,7 @@ int qs_try_apply_fast(qs_register* reg, const double* matrix, size_t rows, size_
 }
 
 int qs_try_apply_all(qs_register* reg, const double* matrix, size_t rows, size_t cols, size_t k, size_t* err) {
+    qs::TraceRange trace("qs_try_apply_all");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if (k != 1) {  // src/register.rs:269-271
         if (err) err[0] = k;
@@ -286,6 +292,7 @@ int qs_try_apply_all(qs_register* reg, const double* matrix, size_t rows, size_t
 
 int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m, const qs_circuit_options* opts,
                      size_t* err) {
+    qs::TraceRange trace("qs_apply_circuit");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if (m > 0 && !gates) return set_err(QS_INVALID_ARGUMENT, "gates is null");
     qs_circuit_options o;
@@ -309,6 +316,7 @@ int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m, const qs_
 
 int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, double* prob0, double* prob1,
                    size_t* err) {
+    qs::TraceRange trace("qs_try_measure");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if (target >= size_t(reg->n)) {  // src/register.rs:299-301
         if (err) err[0] = target;
@@ -334,6 +342,7 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, d
 }
 
 int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, double* prob1, size_t* err) {
+    qs::TraceRange trace("qs_measure_probabilities");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if (target >= size_t(reg->n)) {
         if (err) err[0] = target;
@@ -351,6 +360,7 @@ int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, dou
 }
 
 int qs_inner_product(const qs_register* a, const qs_register* b, double* re, double* im) {
+    qs::TraceRange trace("qs_inner_product");
     if (!a || !b) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if (a->n != b->n) return set_err(QS_INVALID_ARGUMENT, "registers differ in size");
     QS_CUDA(cudaStreamSynchronize(b->stream), "inner sync");
@@ -371,6 +381,7 @@ static bool terms_fit(const qs_pauli_term* terms, size_t nterms, int n) {
 }
 
 int qs_expval_pauli(qs_register* reg, const qs_pauli_term* terms, size_t nterms, double* value) {
+    qs::TraceRange trace("qs_expval_pauli");
     if (!reg || !value || (nterms && !terms)) return set_err(QS_INVALID_ARGUMENT, "null argument");
     if (!terms_fit(terms, nterms, reg->n)) return set_err(QS_INVALID_ARGUMENT, "Pauli term acts on a qubit >= n");
     std::string msg;
@@ -380,6 +391,7 @@ int qs_expval_pauli(qs_register* reg, const qs_pauli_term* terms, size_t nterms,
 
 int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, const double* params, size_t nparams,
                         const qs_pauli_term* terms, size_t nterms, double* energy, double* grad, size_t* err) {
+    qs::TraceRange trace("qs_adjoint_gradient");
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
     if ((m && !gates) || (nparams && !params) || (nterms && !terms))
         return set_err(QS_INVALID_ARGUMENT, "null argument");
@@ -394,6 +406,7 @@ int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, 
 uint64_t qs_launch_count(void) { return qs::g_launches.load(std::memory_order_relaxed); }
 
 int qs_get_state(const qs_register* reg, double* dst) {
+    qs::TraceRange trace("qs_get_state");
     if (!reg || !dst) return set_err(QS_INVALID_ARGUMENT, "null argument");
     const uint64_t N = 1ull << reg->n;
     if (reg->prec == QS_PREC_C128) {
@@ -415,6 +428,7 @@ int qs_get_state(const qs_register* reg, double* dst) {
 }
 
 int qs_set_state(qs_register* reg, const double* src) {
+    qs::TraceRange trace("qs_set_state");
     if (!reg || !src) return set_err(QS_INVALID_ARGUMENT, "null argument");
     const uint64_t N = 1ull << reg->n;
     if (reg->prec == QS_PREC_C128) {
@@ -436,6 +450,7 @@ int qs_set_state(qs_register* reg, const double* src) {
 }
 
 int qs_probabilities(const qs_register* reg, double* dst) {
+    qs::TraceRange trace("qs_probabilities");
     if (!reg || !dst) return set_err(QS_INVALID_ARGUMENT, "null argument");
     const uint64_t N = 1ull << reg->n;
     const uint64_t chunk = std::min<uint64_t>(N, 1ull << 22);

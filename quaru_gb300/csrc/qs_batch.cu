@@ -696,6 +696,7 @@ void plan_circuit(const qs_batch_circuit& q, int T, bool df_ok, BCirc* C, const 
 
 extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, const qs_batch_options* opts,
                                qs_batch** out, size_t* err) {
+    qs::TraceRange trace("qs_batch_create");
     auto fail = [&](int code, const std::string& m) {
         set_last_error_message(m);
         return code;
@@ -946,6 +947,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
 }
 
 extern "C" int qs_batch_run(qs_batch* b, const double* params, double* energies, double* grads) {
+    qs::TraceRange trace("qs_batch_run");
     if (!b || (b->total_params && !params)) {
         set_last_error_message("null argument");
         return QS_INVALID_ARGUMENT;

@@ -8,7 +8,18 @@
 
 #include "qs_internal.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace qs {
+
+// An NVTX range around one public call, named after it (nothing is recorded unless a profiler is
+// attached): sweeps, circuits, measurements, gradients and batch runs show up as ranges in a trace.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 constexpr uint8_t PF_SKIP_DEV = 4;  // PfClass::PF_SKIP as seen by device code
 
