@@ -92,3 +92,30 @@ def test_gate_table_records_point_at_each_gate():
     with pytest.raises(OperationError) as e:
         gate_table([O.hadamard(0), Operation(np.eye(2), [0, 1])])
     assert e.value.kind == "InvalidDimensions" and e.value.payload == (2, 2)
+
+
+def test_param_gate_table_records_point_at_each_gate():
+    """qs_param_gate records (ParamCircuit, Register.adjoint_gradient): kind, parameter index, arity,
+    targets, and the fixed gates' matrices; rotations carry no matrix."""
+    import numpy as np
+
+    from quaru_gb300 import _lib
+    from quaru_gb300 import operation as O
+    from quaru_gb300.register import ParamCircuit, ParamGate
+
+    assert ctypes.sizeof(_lib.QsParamGate) == 32
+    gates = [ParamGate.ry(2, 0), ParamGate.fixed(O.cnot(2, 5)), ParamGate.rz(5, 1),
+             ParamGate.fixed(O.cnx([0, 1], 3)), ParamGate.rx(4, 0)]
+    pc = ParamCircuit(gates)
+    assert len(pc) == len(gates)
+    for rec, g in zip(pc.table, gates):
+        assert int(rec["kind"]) == g.kind
+        k = int(rec["k"])
+        t = np.frombuffer((ctypes.c_size_t * k).from_address(int(rec["targets"])), dtype=np.uintp)
+        if g.kind == _lib.QS_GATE_FIXED:
+            assert list(t) == list(g.op.targets)
+            m = np.frombuffer((ctypes.c_double * (2 * 4 ** k)).from_address(int(rec["matrix"])), dtype=np.float64)
+            assert np.array_equal(m.view(np.complex128).reshape(1 << k, 1 << k), np.asarray(g.op.matrix))
+        else:
+            assert k == 1 and list(t) == [g.target] and int(rec["param"]) == g.param
+            assert int(rec["matrix"]) == 0
