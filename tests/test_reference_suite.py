@@ -1,7 +1,7 @@
 """Quaru's own test suite, restated once and run on two backends.
 
 Sources: tests/register_operation_tests.rs, src/register.rs:437-445,
-examples/shors.rs:434-503, examples/grovers.rs:274-312,
+examples/shors.rs:380-503, examples/grovers.rs:274-312,
 examples/quantum_teleportation.rs:150-164, examples/superdense_coding.rs:84-97.
 proptest strategies over small ranges are enumerated exhaustively; the
 reference's unseeded thread_rng draws are replaced by seeded draws.
@@ -246,6 +246,116 @@ def test_qft_add(B):  # examples/shors.rs:486-503
             r1 = B.from_int(n, b % (1 << n)).apply(g).apply(add)
             r2 = B.from_int(n, (a + b) % (1 << n)).apply(g)
             assert equal_qubits(r1.state, r2.state)
+
+
+def _limit_denominator(m: int, n: int, limit: int) -> tuple[int, int]:  # src/math.rs:55-66
+    """The fraction closest to m/n with denominator at most `limit` (continued fractions)."""
+    a, b, p, q, r, s = n, m % n, 1, 0, m // n, 1
+    while 0 < b and q + a // b * s <= limit:
+        a, b, p, q, r, s = b, a % b, r, s, p + a // b * r, q + a // b * s
+    t, u = p + (limit - q) // s * r, q + (limit - q) // s * s
+    return (r, s) if 2 * b * u <= n else (t, u)
+
+
+def _qubits_for(number: int) -> int:  # ((number + 1) as f64).log2().ceil()
+    return math.ceil(math.log2(number + 1))
+
+
+def find_period_slow(B, number: int, a: int, draw) -> int:  # examples/shors.rs:232-291
+    """3n qubits: H on the first 2n, |1> in the last n, a controlled U (x -> x a^2^i mod N) per
+    counting qubit, the QFT on the counting qubits, measure them, continued fraction of res / 2^2n."""
+    n = _qubits_for(number)
+    reg = B.new([False] * (3 * n))
+    reg.apply(O.hadamard_transform(list(range(2 * n))))
+    reg.apply(O.not_(2 * n))
+    targets = list(range(2 * n, 3 * n))
+    for i in range(2 * n):
+        reg.apply(O.to_controlled(u_gate(targets, number, a, i), i))
+    reg.apply(qft(2 * n))
+    res = 0
+    for i in range(2 * n):
+        if reg.measure(i, draw()):
+            res |= 1 << i
+    return _limit_denominator(res, 2 ** (2 * n) - 1, number - 1)[1]
+
+
+def find_period_fast(B, number: int, a: int, draw) -> int:  # examples/shors.rs:293-357
+    """n + 1 qubits: one control qubit reused 2n times (semiclassical QFT after Parker & Plenio,
+    quant-ph/0001066): H, controlled U (x -> x a^2^(2n-1-i) mod N), the phase R(-2 pi sm), H,
+    measure, reset to |0> on a 1."""
+    n = _qubits_for(number)
+    reg = B.new([False] * (n + 1))
+    reg.apply(O.not_(1))
+    res, sm = 0, 0.0
+    targets = list(range(1, n + 1))
+    for i in range(2 * n):
+        reg.apply(O.hadamard(0))
+        reg.apply(O.to_controlled(u_gate(targets, number, a, 2 * n - 1 - i), 0))
+        phi = complex(math.cos(-2.0 * math.pi * sm), math.sin(-2.0 * math.pi * sm))
+        reg.apply(Operation.new(np.array([[1.0, 0.0], [0.0, phi]], dtype=complex), [0]))
+        reg.apply(O.hadamard(0))
+        m = reg.measure(0, draw())
+        sm /= 2.0
+        if m:
+            reg.apply(O.not_(0))
+            res |= 1 << i
+            sm += 0.25
+    return _limit_denominator(res, 2 ** (2 * n) - 1, number - 1)[1]
+
+
+def _draws(seed: int):
+    rng = np.random.default_rng(seed)
+    return lambda: float(rng.random())
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_period_finder_working(B, fast):  # examples/shors.rs:380-410
+    """For every N < 6 (slow) or < 15 (fast) and every a coprime to N: the period r of a^x mod N is
+    a multiple of the found one in at least 15 of 20 runs (seeded draws)."""
+    for number in range(2, 15 if fast else 6):
+        for a in range(2, number):
+            if math.gcd(number, a) != 1:
+                continue
+            period, a_pow = 1, a
+            while a_pow != 1:
+                a_pow = a_pow * a % number
+                period += 1
+            draw = _draws(1000 * number + a + (500 if fast else 0))
+            ok = 0
+            for _ in range(20):
+                r = (find_period_fast if fast else find_period_slow)(B, number, a, draw)
+                if period % r == 0:
+                    ok += 1
+            assert ok >= 15, (number, a, ok)
+
+
+def shors(B, number: int, rng) -> int:  # examples/shors.rs:96-173 (fast period finder)
+    if number % 2 == 0:
+        return 2
+    for k in range(2, int(math.log2(number)) + 1):  # prime powers c^k
+        c = int(number ** (1.0 / k) + 1e-9)
+        if c ** k == number:
+            return c
+    draw = _draws(int(rng.integers(1 << 30)))
+    while True:
+        a = int(rng.integers(2, number))
+        k = math.gcd(a, number)
+        if k != 1:
+            return k
+        r = find_period_fast(B, number, a, draw)
+        if r % 2 == 0:
+            k = _modpow(a, r // 2, number)
+            if k != number - 1:
+                for f in (math.gcd(k - 1, number), math.gcd(k + 1, number)):
+                    if f != 1 and f != number:
+                        return f
+
+
+def test_shors_working(B):  # examples/shors.rs:412-420
+    rng = np.random.default_rng(15)
+    for number in (4, 6, 8, 9, 10, 12, 14, 15):
+        r = shors(B, number, rng)
+        assert number % r == 0 and 1 < r < number, (number, r)
 
 
 # ---------------------------------------------------------------- examples/grovers.rs tests
