@@ -5,7 +5,9 @@
 //
 // stdin (little-endian): n, T, L (int32); m (int32); per gate: k (int32),
 // k targets (int32), 2^k x 2^k complex (2*4^k doubles); then 2^n complex
-// amplitudes. stdout: 2^n complex amplitudes, the number of stages, the number of register passes.
+// amplitudes. argv: [mode ("pass" or anything else)] [largest gate count per stage].
+// stdout: 2^n complex amplitudes, the number of stages, the number of register passes, the most
+// gates any stage holds.
 #include <algorithm>
 #include <array>
 #include <cstdint>
@@ -248,7 +250,10 @@ int main(int argc, char** argv) {
     }
     std::vector<C> st(size_t(1) << n);
     if (!rd(reinterpret_cast<double*>(st.data()), 2 * st.size())) return 2;
-    const auto stages = qs::plan_tiles(ops, n, T, L, !passes);
+    const int max_ops = argc > 2 ? std::atoi(argv[2]) : qs::kMaxStageOps;
+    const auto stages = qs::plan_tiles(ops, n, T, L, !passes, max_ops);
+    int32_t widest = 0;
+    for (const auto& stage : stages) widest = std::max<int32_t>(widest, int32_t(stage.ops.size()));
     int32_t npasses = 0;
     for (const auto& stage : stages) {
         if (!stage.tiled) {
@@ -290,5 +295,6 @@ int main(int argc, char** argv) {
     int32_t ns = int32_t(stages.size());
     fwrite(&ns, sizeof(ns), 1, stdout);
     fwrite(&npasses, sizeof(npasses), 1, stdout);
+    fwrite(&widest, sizeof(widest), 1, stdout);
     return 0;
 }

@@ -33,16 +33,19 @@ def emulator():
     return EXE
 
 
-def run_emulator(exe, n, T, L, ops, state, mode="exact"):
+def run_emulator(exe, n, T, L, ops, state, mode="exact", max_ops=None, widest=False):
     buf = bytearray(struct.pack("<4i", n, T, L, len(ops)))
     for op in ops:
         t = list(op.targets)
         buf += struct.pack("<i", len(t)) + struct.pack(f"<{len(t)}i", *t)
         buf += np.ascontiguousarray(np.asarray(op.matrix, dtype=np.complex128)).tobytes()
     buf += np.ascontiguousarray(state, dtype=np.complex128).tobytes()
-    r = subprocess.run([str(exe), mode], input=bytes(buf), capture_output=True, check=True)
+    argv = [str(exe), mode] + ([str(max_ops)] if max_ops else [])
+    r = subprocess.run(argv, input=bytes(buf), capture_output=True, check=True)
     out = np.frombuffer(r.stdout[: 16 << n], dtype=np.complex128)
-    stages, passes = struct.unpack("<2i", r.stdout[16 << n:])
+    stages, passes, most = struct.unpack("<3i", r.stdout[16 << n:])
+    if widest:
+        return out, stages, most
     return (out, stages, passes) if mode == "pass" else (out, stages)
 
 
@@ -138,3 +141,22 @@ def test_fused_blocks_reproduce_gate_by_gate(fuser, oracle_mod, W):
         o.apply_sequence([(g.matrix, g.targets) for g in ops])
         assert nblocks < len(ops)
         assert np.max(np.abs(got - o.state)) < 1e-12, name
+
+
+@pytest.mark.parametrize("max_ops", [4, 32])
+def test_stage_gate_cap(emulator, oracle_mod, max_ops):
+    """plan_tiles with a cap on the gates per stage (the adjoint's reverse sweep plans with 32): no
+    stage exceeds it, and the capped plan still gives the oracle's amplitudes exactly."""
+    for name, n, ops in cases():
+        rng = np.random.default_rng(len(ops) + 11)
+        st = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        st /= np.linalg.norm(st)
+        o = oracle_mod.OracleRegister.from_int(n, 0)
+        o.state = st.copy()
+        o.apply_sequence([(g.matrix, g.targets) for g in ops])
+        got, stages, most = run_emulator(emulator, n, min(11, n), min(5, n), ops, st, max_ops=max_ops, widest=True)
+        assert 0 < most <= max_ops, (name, most)
+        _, uncapped = run_emulator(emulator, n, min(11, n), min(5, n), ops, st)
+        assert stages >= uncapped, name
+        bad = np.nonzero(~((got.view(np.float64) == o.state.view(np.float64))))[0]
+        assert bad.size == 0, f"{name}: {bad.size} values differ"
