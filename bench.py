@@ -7,6 +7,9 @@ matching (15 CNOTs) — on a complex128 state (16 GiB, far larger than the
 129 MB L2, so no flush is needed between steps). One step = one layer
 (45 gates), applied through the reference-facing call (qs_try_apply_fast, one
 call per gate, matrices from host memory). Synthetic seeded gates (SplitMix64).
+The headline arithmetic is plain FP64 (fused multiply-add, `--arith fma`); the
+other arithmetic forms of the dense 1-qubit sweep are timed beside it under
+their own names (`dense1_forms`).
 
 metric: HBM GB/s per gate sweep = sum over gates of the algorithmic bytes
 (one read + one write of every amplitude a gate changes: 2*N*16 for a dense
@@ -14,7 +17,10 @@ metric: HBM GB/s per gate sweep = sum over gates of the algorithmic bytes
 
 `--impl reference` times the reference algorithm on the host (the C
 restatement of Register::try_apply_fast in oracle/, single-threaded like the
-reference) on the same metric.
+reference) on the same metric, with the same sample the GPU arm's
+`cpu_baseline` uses (whole layers of the family at CPU_QUBITS qubits).
+`--cpu-sweep` runs the family (40 layers) on the host at n = 12, 14, ... until
+a size exceeds `--cpu-limit` seconds.
 """
 from __future__ import annotations
 
@@ -124,23 +130,77 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU (reference algorithm) timing
-def cpu_reference_gbps(n: int, layers, budget_s: float, max_gates: int | None = None) -> dict:
-    """Time the oracle's restatement of Register::try_apply_fast, one gate after another, for about budget_s."""
+CPU_QUBITS = 22   # host sample size: a 64 MiB state (plus the reference's per-gate clone), beyond the host caches
+CPU_SWEEP_LAYERS = 40
+
+
+def cpu_layers_gbps(n: int, layers, budget_s: float | None = None, limit_s: float | None = None) -> dict:
+    """Time the oracle's restatement of Register::try_apply_fast (clone + per-tuple gather, mat-vec,
+    scatter; 1 thread like the reference) over whole layers of the family, one gate after another.
+    budget_s: stop after the first layer that ends past it. limit_s: abandon the run once it passes
+    it (the run then counts as not completed)."""
     from oracle.oracle import OracleRegister
 
     reg = OracleRegister.from_int(n, 0)
-    gates = [g for layer in layers for g in layer]
-    done, nbytes = 0, 0.0
+    done_layers, gates, nbytes = 0, 0, 0.0
     t0 = time.perf_counter()
-    for g in gates:
-        reg.try_apply_fast(g.matrix, g.targets)
-        done += 1
-        nbytes += gate_bytes(g, n, 16)
-        el = time.perf_counter() - t0
-        if el >= budget_s or (max_gates and done >= max_gates):
+    completed = True
+    for layer in layers:
+        for g in layer:
+            reg.try_apply_fast(g.matrix, g.targets)
+            gates += 1
+            nbytes += gate_bytes(g, n, 16)
+            if limit_s is not None and time.perf_counter() - t0 > limit_s:
+                completed = False
+                break
+        if not completed:
+            break
+        done_layers += 1
+        if budget_s is not None and time.perf_counter() - t0 >= budget_s:
             break
     el = time.perf_counter() - t0
-    return {"gbps": nbytes / el / 1e9, "gates": done, "seconds": el, "gates_per_s": done / el}
+    return {"qubits": n, "layers": done_layers, "gates": gates, "seconds": el, "gates_per_s": gates / el,
+            "gbps": nbytes / el / 1e9, "completed": completed}
+
+
+def cpu_c1_seconds() -> dict:
+    """The 12-qubit, 200-gate parity configuration on the oracle, measuring every qubit."""
+    from oracle.oracle import OracleRegister
+    from quaru_gb300.workloads import config1_circuit
+
+    c = config1_circuit()
+    t0 = time.perf_counter()
+    reg = OracleRegister.from_int(c.n, 0)
+    for g in c.gates:
+        reg.try_apply_fast(g.matrix, g.targets)
+    bits = [int(reg.measure(t, c.draws[t])) for t in range(c.n)]
+    return {"seconds": time.perf_counter() - t0, "gates": len(c.gates), "bitstring": "".join(map(str, bits))}
+
+
+def cpu_sweep(limit_s: float, start: int = 12, stop: int = 30) -> dict:
+    """The family at n = start, start+2, ... (40 layers each) until a size runs past limit_s."""
+    from quaru_gb300.workloads import layered_circuit, seed_for
+
+    runs = []
+    largest = None
+    for n in range(start, stop + 1, 2):
+        r = cpu_layers_gbps(n, layered_circuit(n, CPU_SWEEP_LAYERS, seed_for(2)), limit_s=limit_s)
+        runs.append(r)
+        if not r["completed"]:
+            break
+        largest = r
+    return {"limit_s": limit_s, "layers": CPU_SWEEP_LAYERS, "runs": runs,
+            "largest_completed_qubits": largest["qubits"] if largest else None,
+            "largest_completed_gbps": largest["gbps"] if largest else None,
+            "largest_completed_gates_per_s": largest["gates_per_s"] if largest else None}
+
+
+def cpu_sample_text(n: int, r: dict) -> str:
+    return (f"{n}-qubit instance of the layered family ({r['layers']} whole layers, {r['gates']} gates, "
+            f"{r['seconds']:.1f} s): the oracle's C restatement of Register::try_apply_fast (clone + per-tuple "
+            f"gather/mat-vec/scatter), 1 thread as in the reference; GB/s per sweep does not depend on the "
+            f"size once the state exceeds the host caches, and the 30-qubit state plus its per-gate clone "
+            f"would need 32 GiB of host memory")
 
 
 def run_reference(args) -> None:
@@ -149,47 +209,67 @@ def run_reference(args) -> None:
         return
     from quaru_gb300.workloads import layered_circuit, seed_for
 
-    n = args.ref_qubits
-    layers = layered_circuit(n, 2, seed_for(3))
-    gates = [g for layer in layers for g in layer]
-    from oracle.oracle import OracleRegister
-
-    reg = OracleRegister.from_int(n, 0)
-    per_step = []
-    total_bytes = 0.0
-    total_t = 0.0
-    gi = 0
-    for step in range(args.warmup + args.steps):
-        g = gates[gi % len(gates)]
-        gi += 1
-        t0 = time.perf_counter()
-        reg.try_apply_fast(g.matrix, g.targets)
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            per_step.append(dt)
-            total_bytes += gate_bytes(g, n, 16)
-            total_t += dt
-    value = total_bytes / total_t / 1e9
-    sample = (f"{n}-qubit instance of the layered family (the {args.qubits}-qubit state and its per-gate clone "
-              f"would need {2 * (16 << args.qubits) / 2**30:.0f} GiB of host memory; GB/s per sweep does not depend "
-              f"on the size once the state exceeds the caches), one gate per step (Haar 1q or CNOT), oracle/ C "
-              f"restatement of Register::try_apply_fast (clone + per-tuple gather/mat-vec/scatter), 1 thread as "
-              f"in the reference")
+    n = args.cpu_qubits
+    layers = layered_circuit(n, args.warmup + args.steps, seed_for(3))
+    cpu_layers_gbps(n, layers[: args.warmup])  # warm-up layers, untimed
+    r = cpu_layers_gbps(n, layers[args.warmup:])
+    value = r["gbps"]
     nw = args.qubits
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(1, args.steps),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"{nw}-qubit layered random circuit (per layer: Haar 1q on all {nw} qubits + "
                                f"{nw // 2} CNOTs on a random perfect matching), one layer per step",
                    "qubits": nw, "precision": "c128", "sample_qubits": n, "parallelism": "single (host)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": cpu_sample_text(n, r) + "; one layer per step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def run_cpu_sweep(args) -> None:
+    out = {"cpu_sweep": cpu_sweep(args.cpu_limit), "c1": cpu_c1_seconds(), "cores": 1,
+           "host_cpus": os.cpu_count(), "machine": os.uname().machine}
+    print(json.dumps(out), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
+def ARITH_CODES(q) -> dict:
+    return {"exact": q.QS_ARITH_EXACT, "fma": q.QS_ARITH_FMA, "df64": q.QS_ARITH_DF64, "fx64": q.QS_ARITH_FX64}
+
+
+# what each arithmetic form of a complex128 dense gate computes in
+ARITH_DTYPE = {"exact": "f64", "fma": "f64", "df64": "f32x2 (double-float)",
+               "fx64": "int64 fixed point, rounded once to f64 (FP64-accurate)"}
+
+
+def dense1_forms(q, torch, reg, layers, n: int, peak: float, count: int = 8) -> dict:
+    """The dense 1-qubit sweep (k_dense1) in every arithmetic form on the same register: CUDA events
+    around each of `count` Haar gates after 2 warm-up gates; GB/s = 2 * 2^n * 16 / average time."""
+    haar = [g for layer in layers for g in layer if is_haar(g)][: count + 2]
+    stream = torch.cuda.ExternalStream(reg.stream)
+    out = {}
+    for name, code in ARITH_CODES(q).items():
+        reg.set_arith(code)
+        for g in haar[:2]:
+            reg.try_apply_fast(g)
+        evs = []
+        for g in haar[2:]:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            reg.try_apply_fast(g)
+            b.record(stream)
+            evs.append((a, b))
+        reg.synchronize()
+        ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+        gbs = 2.0 * (1 << n) * 16 / (ms / 1e3) / 1e9
+        out[name] = {"ms": ms, "gbs": gbs, "frac_of_measured_hbm": gbs / peak, "arith": ARITH_DTYPE[name]}
+    return out
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -209,7 +289,7 @@ def run_ours(args) -> None:
 
     lib = _lib.load()
     n = args.qubits
-    arith = {"exact": q.QS_ARITH_EXACT, "fma": q.QS_ARITH_FMA, "df64": q.QS_ARITH_DF64}[args.arith]
+    arith = ARITH_CODES(q)[args.arith]
     prec = q.QS_PREC_C64 if args.precision == "c64" else q.QS_PREC_C128
     amp = 8 if prec == q.QS_PREC_C64 else 16
     nlayers = max(args.warmup + args.steps, 1)
@@ -288,7 +368,22 @@ def run_ours(args) -> None:
         barrier()
         fs = f0.elapsed_time(f1) / 1e3
         fused = {"gates_per_s": len(fl) / fs, "ms_per_step": 1e3 * fs / args.steps,
-                 "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0)}
+                 "speedup_vs_unfused": dev_s / fs, "launches": int(lib.qs_launch_count() - l0),
+                 "tile_qubits": q.circuit_autotune(n, prec, arith, 1)["tile_qubits"]}
+        # fuse = 3: the autotuned form
+        reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=3)
+        barrier()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        l0 = lib.qs_launch_count()
+        a0.record(stream)
+        reg.apply_gates(fl, fuse=3)
+        a1.record(stream)
+        barrier()
+        ats = a0.elapsed_time(a1) / 1e3
+        fused["autotuned"] = {"choice": q.circuit_autotune(n, prec, arith, 3), "gates_per_s": len(fl) / ats,
+                              "ms_per_step": 1e3 * ats / args.steps, "speedup_vs_unfused": dev_s / ats,
+                              "launches": int(lib.qs_launch_count() - l0)}
         if prec == q.QS_PREC_C128:
             # dense fused blocks at the automatic width (double-float arithmetic: 3-qubit blocks)
             b0 = torch.cuda.Event(enable_timing=True)
@@ -303,7 +398,7 @@ def run_ours(args) -> None:
             bs = b0.elapsed_time(b1) / 1e3
             fused["blocks"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
                                "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0),
-                               "max_width": 3 if args.arith == "df64" else 2}
+                               "max_width": q.circuit_autotune(n, prec, arith, 2)["max_width"]}
         if prec == q.QS_PREC_C64:
             # dense 5-qubit blocks as 3xTF32 tensor-core GEMMs
             b0 = torch.cuda.Event(enable_timing=True)
@@ -319,6 +414,15 @@ def run_ours(args) -> None:
             fused["blocks_tf32x3"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
                                       "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0)}
 
+    peak, peak_kind = read_peaks()
+    forms = None
+    if prec == q.QS_PREC_C128 and not args.no_forms:
+        forms = dense1_forms(q, torch, reg, layers, n, peak)
+        reg.set_arith(arith)
+    del reg
+    torch.cuda.synchronize()
+    tuned = None if args.no_fused else autotune_section(q, args)
+    meas = None if args.no_measure else measure_section(q, torch, args)
     widths = None if args.no_widths else width_section(q, torch, args)
     precision = None if args.no_precision else precision_section(q, torch, args)
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
@@ -336,7 +440,6 @@ def run_ours(args) -> None:
     avg_haar_s = statistics.mean(haar_ms) / 1e3 if haar_ms else float("nan")
     per_launch_bytes = 2.0 * (1 << n) * amp
     achieved = per_launch_bytes / avg_haar_s / 1e9
-    peak, peak_kind = read_peaks()
     flops_per_launch = (1 << n) * 8 * 2.0  # 8 FMAs per amplitude for a dense complex 2x2
     gates_per_step = len(layer(0))
 
@@ -347,16 +450,18 @@ def run_ours(args) -> None:
 
     cpu = None
     if world == 1 and not args.no_cpu:
-        r = cpu_reference_gbps(args.cpu_qubits, layered_circuit(args.cpu_qubits, 2, seed_for(3)), args.cpu_budget)
-        cpu = {"value": r["gbps"], "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_qubits}-qubit instance of the layered family, first {r['gates']} gates "
-                         f"({r['seconds']:.1f} s), oracle/ C restatement of Register::try_apply_fast, 1 thread "
-                         f"(the reference is single-threaded)"}
+        # the same sample as `--impl reference`: whole layers at CPU_QUBITS qubits, same seed
+        n_cpu = args.cpu_qubits
+        r = cpu_layers_gbps(n_cpu, layered_circuit(n_cpu, 40, seed_for(3)), budget_s=args.cpu_budget)
+        cpu = {"value": r["gbps"], "unit": UNIT, "cores": 1, "kind": "port", "sample": cpu_sample_text(n_cpu, r),
+               "gates_per_s": r["gates_per_s"], "host_cpus": os.cpu_count(),
+               "sweep": cpu_sweep(args.cpu_limit, stop=n_cpu), "c1": cpu_c1_seconds()}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == q.QS_PREC_C64 else "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == q.QS_PREC_C64 else ARITH_DTYPE[args.arith],
         "data": "synthetic (seeded Haar 1q + CNOT matchings, SplitMix64)",
         "config": {"workload": f"{n}-qubit layered random circuit (per layer: Haar 1q on all {n} qubits + "
                                f"{n // 2} CNOTs on a random perfect matching), one layer per step",
@@ -374,6 +479,9 @@ def run_ours(args) -> None:
                      "fp64_equivalent_tflops": flops_per_launch / avg_haar_s / 1e12,
                      "fp64_pipe_peak_tflops_measured": FP64_PEAK_TFLOPS_MEASURED},
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
+        "dense1_forms": forms,
+        "autotune": tuned,
+        "measure": meas,
         "clocks": clk,
         "fused": fused,
         "fusion_widths": widths,
@@ -386,6 +494,58 @@ def run_ours(args) -> None:
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def autotune_section(q, args) -> dict:
+    """The fusion autotuner at the bench's size: for each precision / arithmetic, the form it picks for
+    qs_apply_circuit (fuse = 3: single sweeps, stages with their tile size, or dense blocks with their
+    width) and the stand-in workload's time under every candidate (re-timed here)."""
+    out = {}
+    for name, prec, arith in (("c128_fma", q.QS_PREC_C128, q.QS_ARITH_FMA), ("c128_fx64", q.QS_PREC_C128, q.QS_ARITH_FX64),
+                              ("c128_df64", q.QS_PREC_C128, q.QS_ARITH_DF64), ("c64", q.QS_PREC_C64, q.QS_ARITH_FMA)):
+        out[name] = q.circuit_autotune(args.qubits, prec, arith, 3, retune=True)
+    return out
+
+
+def measure_section(q, torch, args) -> dict:
+    """Measurement: the 12-qubit, 200-gate parity configuration end to end on the GPU (gates one call
+    each, then every qubit measured in one qs_measure_sequence call, complex128 exact arithmetic:
+    reference-order sums), and measuring all qubits of a dense 30-qubit complex128 state as one
+    sequence (each pass reads only the live subspace and fuses the next qubit's sums) against one
+    qs_try_measure call per qubit."""
+    from quaru_gb300.workloads import config1_circuit, flatten, layered_circuit, seed_for
+
+    c = config1_circuit()
+    reps = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        r = q.Register.from_int(c.n, 0)
+        for g in c.gates:
+            r.try_apply_fast(g)
+        bits = r.measure_sequence(list(range(c.n)), c.draws)
+        reps.append(time.perf_counter() - t0)
+        del r
+    out = {"c1": {"workload": "12 qubits, 200 gates, measure all 12 (seeded draws)", "ms": 1e3 * min(reps),
+                  "bitstring": "".join(str(int(b)) for b in bits)}}
+    n = args.qubits
+    a = q.Register.from_int(n, 0)
+    a.set_arith(q.QS_ARITH_FMA)
+    a.apply_gates(flatten(layered_circuit(n, 1, seed_for(3))))
+    b = a.clone()
+    draws = [float(x) for x in np.random.default_rng(30).uniform(size=n)]
+    a.synchronize()
+    b.synchronize()
+    t0 = time.perf_counter()
+    seq = a.measure_sequence(list(range(n)), draws)
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    one = [b.measure(t, d) for t, d in enumerate(draws)]
+    t_one = time.perf_counter() - t0
+    out[f"measure_all_{n}q"] = {"sequence_ms": 1e3 * t_seq, "per_qubit_calls_ms": 1e3 * t_one,
+                                "speedup": t_one / t_seq, "same_outcomes": seq == one,
+                                "first_pass_bytes": 3.0 * (1 << n) * 16}
+    del a, b
+    return out
 
 
 def width_section(q, torch, args) -> dict:
@@ -428,21 +588,23 @@ def width_section(q, torch, args) -> dict:
 
 
 def precision_section(q, torch, args) -> dict:
-    """The layered family at the bench's size for 40 layers: complex128 gate by gate (the plain FP64
-    form, the bench's arithmetic) against complex64 fused stages (register passes, and 5-qubit dense
-    blocks as 3xTF32 tensor-core GEMMs), with 1 - F = 1 - |<mixed|fp64>|^2 / (<mixed|mixed><fp64|fp64>)
-    accumulated in FP64 on the GPU after every 10 layers, and the gates/s of each form."""
+    """The layered family at the bench's size for 40 layers: complex128 gate by gate in FP64 FMA
+    arithmetic (the plain FP64 form) against complex128 double-float sweeps and complex64 fused stages
+    (register passes, and 5-qubit dense blocks as 3xTF32 tensor-core GEMMs), with
+    1 - F = 1 - |<x|fp64>|^2 / (<x|x><fp64|fp64>) accumulated in FP64 on the GPU after every 10
+    layers, and the gates/s of each form."""
     from quaru_gb300.workloads import flatten, layered_circuit, seed_for
 
     n = args.qubits
     layers = layered_circuit(n, 40, seed_for(3))
     torch.cuda.synchronize()
     regs = {"fp64_plain": q.Register.from_int(n, 0),
+            "c128_df64": q.Register.from_int(n, 0),
             "c64_passes": q.Register.from_int(n, 0, precision=q.QS_PREC_C64),
             "c64_blocks_tf32x3": q.Register.from_int(n, 0, precision=q.QS_PREC_C64)}
-    regs["fp64_plain"].set_arith({"exact": q.QS_ARITH_EXACT, "fma": q.QS_ARITH_FMA,
-                                  "df64": q.QS_ARITH_DF64}[args.arith])
-    fuse = {"fp64_plain": 0, "c64_passes": 1, "c64_blocks_tf32x3": 2}
+    regs["fp64_plain"].set_arith(q.QS_ARITH_FMA)  # the plain FP64 form: FP64 fused multiply-add
+    regs["c128_df64"].set_arith(q.QS_ARITH_DF64)
+    fuse = {"fp64_plain": 0, "c128_df64": 0, "c64_passes": 1, "c64_blocks_tf32x3": 2}
     secs = {k: 0.0 for k in regs}
     gates = 0
     checkpoints = []
@@ -461,7 +623,7 @@ def precision_section(q, torch, args) -> dict:
         ref = regs["fp64_plain"]
         nref = ref.inner_product(ref).real
         cp = {"layers": 10 * (k + 1)}
-        for name in ("c64_passes", "c64_blocks_tf32x3"):
+        for name in ("c128_df64", "c64_passes", "c64_blocks_tf32x3"):
             r = regs[name]
             f = abs(r.inner_product(ref)) ** 2 / (nref * r.inner_product(r).real)
             cp[f"one_minus_fidelity_{name}"] = 1.0 - f
@@ -469,7 +631,9 @@ def precision_section(q, torch, args) -> dict:
     out = {"workload": f"{n}-qubit layered family, 40 layers ({gates} gates), same seed as the main run",
            "checkpoints": checkpoints,
            "gates_per_s": {k: gates / v for k, v in secs.items()}}
-    out["mixed_vs_fp64_gates_per_s"] = {k: secs["fp64_plain"] / secs[k] for k in ("c64_passes", "c64_blocks_tf32x3")}
+    out["mixed_vs_fp64_gates_per_s"] = {k: secs["fp64_plain"] / secs[k]
+                                        for k in ("c128_df64", "c64_passes", "c64_blocks_tf32x3")}
+    out["fp64_plain_arith"] = "FP64 fused multiply-add, one sweep per gate"
     del regs
     return out
 
@@ -624,11 +788,17 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--precision", choices=["c128", "c64"], default="c128")
-    ap.add_argument("--arith", choices=["exact", "fma", "df64"], default="df64")
-    ap.add_argument("--cpu-qubits", type=int, default=24)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--ref-qubits", type=int, default=26)
+    ap.add_argument("--arith", choices=["exact", "fma", "df64", "fx64"], default="fma",
+                    help="arithmetic of the headline sweep (default: plain FP64, fused multiply-add)")
+    ap.add_argument("--cpu-qubits", type=int, default=CPU_QUBITS,
+                    help="size of the host sample (cpu_baseline and --impl reference)")
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of the host sample (whole layers)")
+    ap.add_argument("--cpu-limit", type=float, default=20.0,
+                    help="per-size time limit of the host sweep over n = 12, 14, ... (--cpu-sweep: default 600)")
+    ap.add_argument("--cpu-sweep", action="store_true", help="run only the host sweep and print its JSON")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the per-arithmetic dense 1-qubit timing")
+    ap.add_argument("--no-measure", action="store_true", help="skip the measurement section")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused (tiled) circuit timing")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient section")
     ap.add_argument("--no-precision", action="store_true", help="skip the 40-layer precision-form section")
@@ -638,7 +808,11 @@ def main() -> None:
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")
-    if args.impl == "reference":
+    if args.cpu_sweep:
+        if "--cpu-limit" not in sys.argv:
+            args.cpu_limit = 600.0
+        run_cpu_sweep(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.kernels:
         run_kernels(args)

@@ -52,6 +52,10 @@ extern "C" {
 #define QS_ARITH_FMA 1   /* FP64 fused multiply-add; within 1e-15 relative per gate */
 #define QS_ARITH_DF64 2  /* double-float arithmetic on the FP32 pipe for dense gates;
                             ~2^-47 relative per gate; permutation/diagonal gates stay exact */
+#define QS_ARITH_FX64 3  /* FP64-accurate fixed-point arithmetic on the integer pipes for dense
+                            1-qubit gates: each output is an exact-to-2^-55 integer dot product
+                            rounded once to double (error <= ulp/2 + 2^-55 max|u| max|x|, below
+                            the FP64 FMA form's); other gates and fused stages use FP64 FMA */
 
 typedef struct qs_register qs_register;
 
@@ -114,13 +118,39 @@ typedef struct qs_gate {
 typedef struct qs_circuit_options {
     int fuse;        /* 0: one sweep per gate; 1: cache-blocked stages (bit-identical to 0
                         under QS_ARITH_EXACT); 2: dense fused blocks (complex64 registers:
-                        3xTF32 tensor-core blocks) */
-    int max_width;   /* widest fused dense block, 2..5 (fuse == 2); 0 = automatic: 5 on complex64
-                        registers (tensor-core blocks), 3 on complex128 with QS_ARITH_DF64 (the
-                        widest double-float dense kernel), 2 otherwise (FP64 blocks) */
-    int tile_qubits; /* qubits per shared-memory tile for fuse >= 1; 0 = automatic */
+                        3xTF32 tensor-core blocks); 3: the autotuner picks 0, 1 (and its tile
+                        size) or 2 (and its width) */
+    int max_width;   /* widest fused dense block, 2..5 (fuse == 2); 0 = autotuned (see
+                        qs_circuit_autotune) */
+    int tile_qubits; /* qubits per shared-memory tile for fuse == 1; 0 = autotuned */
     int reserved;
 } qs_circuit_options;
+
+/* The fusion autotuner (the counterpart of choosing QuantumCircuit reduction
+ * passes by hand, src/operation.rs:114-269): the candidates of `fuse` (1: tile
+ * sizes of stages; 2: block widths 2..5; 3: both, plus one sweep per gate) are
+ * timed once per (n, precision, arith, fuse) on a scratch register running a
+ * seeded stand-in workload of the benchmarks' family (two layers of random
+ * dense 1-qubit gates on every qubit and CNOTs on a random matching) at
+ * min(n, 26) qubits; the fastest is kept in memory and in the autotune cache
+ * file (QS_AUTOTUNE_CACHE, default ~/.cache/quaru_gb300_autotune.txt). Later
+ * qs_apply_circuit calls with fuse == 3, or fuse 1 / 2 with a zero tile size /
+ * width, use that choice; QS_AUTOTUNE=off selects the fixed rules instead
+ * (tile qubits min(11 or 12, max(8 or 9, n - 7)) for complex128 / complex64;
+ * width 5 complex64, 3 double-float, 2 otherwise; fuse 3 -> 1). qs_circuit_autotune
+ * returns the choice and, when it timed the candidates (first use, or
+ * retune != 0), each candidate's time. It needs a device but no register. */
+#define QS_AUTOTUNE_MAX_CANDIDATES 16
+typedef struct qs_autotune_report {
+    int fuse, max_width, tile_qubits;  /* the choice */
+    int from_cache;                     /* 1: taken from the cache, no timings below */
+    int count;                          /* candidates timed */
+    int cand_fuse[QS_AUTOTUNE_MAX_CANDIDATES];
+    int cand_width[QS_AUTOTUNE_MAX_CANDIDATES];
+    int cand_tile[QS_AUTOTUNE_MAX_CANDIDATES];
+    double cand_ms[QS_AUTOTUNE_MAX_CANDIDATES];
+} qs_autotune_report;
+int qs_circuit_autotune(size_t n, int precision, int arith, int fuse, int retune, qs_autotune_report* out);
 
 /* The operations loop of Register::apply_circuit (src/register.rs:345-350):
  * applies gates[0..m) in order. Every gate is validated before any is
@@ -134,13 +164,30 @@ int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m,
 /* Register::try_measure (src/register.rs:297-342) with the uniform draw in
  * [0, 1) supplied by the caller (the reference's thread_rng, :317-318, cannot
  * be seeded). outcome = draw > prob_0 (:321). prob0/prob1 are nullable and
- * receive the FP64 probability sums before the collapse. */
+ * receive the FP64 probability sums the decision used. Complex128 registers in
+ * QS_ARITH_EXACT with n <= 20 add the squares in index order as the reference
+ * does (:306-315), so sums, outcome and collapsed state are bit-identical to
+ * it; larger registers and the other forms use a fixed-order parallel tree
+ * (within 1e-14). The collapse divides by sqrt(prob) correctly rounded (:337).
+ * Qubits measured since their last gate stay collapsed: later measurements
+ * read only the amplitudes that can still be non-zero. */
 int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
                    double* prob0, double* prob1, size_t* err);
 
-/* The probability sums of try_measure (src/register.rs:303-315) without the
- * draw and the collapse: p0 = sum |a_i|^2 over target bit 0, p1 over bit 1,
- * FP64 on the GPU. The state is left unchanged. */
+/* Register::measure_circuit (src/register.rs:371-377): try_measure of
+ * targets[0..m) in order with draws[0..m), outcomes into outcomes[0..m),
+ * probability sums into prob0s/prob1s (nullable). Every target is checked
+ * before any work (InvalidTarget, err[2] = its index). Each collapse pass also
+ * sums the next target's probabilities over the kept amplitudes, and each pass
+ * reads only the live subspace, so measuring all n qubits costs about two
+ * sweeps of the state instead of 2n. */
+int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
+                        double* prob0s, double* prob1s, size_t* err);
+
+/* The probability sums of a measurement (src/register.rs:303-315) without the
+ * draw and the collapse: p0 = sum |a_i|^2 over target bit 0, p1 over bit 1, a
+ * fixed-order parallel FP64 tree over the whole state (within 1e-14 of the
+ * reference's sequential sum). The state is left unchanged. */
 int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, double* prob1, size_t* err);
 
 /* For callers that cannot allocate device memory. No counterpart in the
@@ -156,10 +203,14 @@ int qs_measure_probabilities(qs_register* reg, size_t target, double* prob0, dou
  * Allocates nothing: per-block partial sums go to a 64 KiB file-scope
  * __device__ array that every GPU loading this library holds until exit, so
  * any n in 1..40 fits; a request needing more scratch than that is rejected
- * with QS_INVALID_ARGUMENT. The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. Every call shares the array: calls that overlap on the
- * GPU (other streams, other host threads) race and must be serialised. */
+ * with QS_INVALID_ARGUMENT, and so is a state pointer not aligned to its
+ * amplitude size (16 or 8 bytes) or an out pointer not aligned to 8 bytes.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ * first call before any stream capture, and do not reset a device
+ * (cudaDeviceReset) that later calls use, which would leave the kept address
+ * stale. Every call shares the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised. */
 int qs_measure_probabilities_noalloc(const void* state, size_t n, int precision, size_t target,
                                      double* out, void* stream, size_t* err);
 

@@ -5,12 +5,12 @@ include/quaru_gpu.h); this package is the host-side mirror of the reference's
 Rust API (Register, Operation, the gate constructors) over that ABI.
 """
 from . import _lib
-from ._lib import (QS_ARITH_DF64, QS_ARITH_EXACT, QS_ARITH_FMA, QS_PREC_C64, QS_PREC_C128)
+from ._lib import (QS_ARITH_DF64, QS_ARITH_EXACT, QS_ARITH_FMA, QS_ARITH_FX64, QS_PREC_C64, QS_PREC_C128)
 from .operation import Operation
-from .register import EngineError, OperationError, ParamCircuit, ParamGate, PauliSum, Register
+from .register import EngineError, OperationError, ParamCircuit, ParamGate, PauliSum, Register, circuit_autotune
 
 __all__ = ["Register", "ParamGate", "ParamCircuit", "PauliSum", "Operation", "OperationError", "EngineError", "QS_PREC_C128", "QS_PREC_C64",
-           "QS_ARITH_EXACT", "QS_ARITH_FMA", "QS_ARITH_DF64"]
+           "QS_ARITH_EXACT", "QS_ARITH_FMA", "QS_ARITH_DF64", "QS_ARITH_FX64", "circuit_autotune"]
 
 
 def version() -> str:

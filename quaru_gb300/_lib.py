@@ -31,6 +31,7 @@ QS_PREC_C64 = 1
 QS_ARITH_EXACT = 0
 QS_ARITH_FMA = 1
 QS_ARITH_DF64 = 2
+QS_ARITH_FX64 = 3
 
 # Every symbol include/quaru_gpu.h declares, with (restype, argtypes).
 _P = ctypes.POINTER
@@ -71,6 +72,16 @@ class QsBatchOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("chunk_log2", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
                 ("arith", ctypes.c_int)]
 
+AUTOTUNE_MAX = 16
+
+
+class QsAutotuneReport(ctypes.Structure):
+    _fields_ = [("fuse", ctypes.c_int), ("max_width", ctypes.c_int), ("tile_qubits", ctypes.c_int),
+                ("from_cache", ctypes.c_int), ("count", ctypes.c_int),
+                ("cand_fuse", ctypes.c_int * AUTOTUNE_MAX), ("cand_width", ctypes.c_int * AUTOTUNE_MAX),
+                ("cand_tile", ctypes.c_int * AUTOTUNE_MAX), ("cand_ms", ctypes.c_double * AUTOTUNE_MAX)]
+
+
 SIGNATURES = {
     "qs_register_new": (_i, [_P(ctypes.c_uint8), _sz, _i, _P(_vp)]),
     "qs_register_from_int": (_i, [_sz, _sz, _i, _P(_vp)]),
@@ -85,6 +96,8 @@ SIGNATURES = {
     "qs_apply_circuit": (_i, [_vp, _P(QsGate), _sz, _P(QsCircuitOptions), _sp]),
     "qs_try_measure": (_i, [_vp, _sz, ctypes.c_double, _P(_i), _dp, _dp, _sp]),
     "qs_measure_probabilities": (_i, [_vp, _sz, _dp, _dp, _sp]),
+    "qs_measure_sequence": (_i, [_vp, _sp, _sz, _dp, _P(_i), _dp, _dp, _sp]),
+    "qs_circuit_autotune": (_i, [_sz, _i, _i, _i, _i, _P(QsAutotuneReport)]),
     "qs_measure_probabilities_noalloc": (_i, [_vp, _sz, _i, _sz, _vp, _vp, _sp]),
     "qs_inner_product": (_i, [_vp, _vp, _dp, _dp]),
     "qs_expval_pauli": (_i, [_vp, _P(QsPauliTerm), _sz, _dp]),

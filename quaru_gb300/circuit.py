@@ -119,12 +119,15 @@ class QuantumCircuit:
             ext = np.kron(eye, a.matrix) if a.targets[0] == b.targets[0] else np.kron(a.matrix, eye)
             m = b.matrix @ ext
         else:
-            targets = list(a.targets)
             if len(a.targets) == len(b.targets):
-                m = a.matrix @ b.matrix
-            else:
-                ext = np.kron(eye, b.matrix) if b.targets[0] == a.targets[0] else np.kron(b.matrix, eye)
-                m = a.matrix @ ext
+                # The reference multiplies op1 (2^k x 2^k) by kron(eye(2), op2) (2^(k+1) square) here
+                # too, and ndarray's dot panics on the shape mismatch (src/operation.rs:166-174): two
+                # overlapping operations of equal arity cannot be combined.
+                raise RuntimeError(f"Cannot combine operations of equal arity {len(a.targets)} on targets "
+                                   f"{list(a.targets)} and {list(b.targets)}: shapes do not match")
+            targets = list(a.targets)
+            ext = np.kron(eye, b.matrix) if b.targets[0] == a.targets[0] else np.kron(b.matrix, eye)
+            m = a.matrix @ ext
         return Operation.new(m, targets)
 
     def reduce_circuit_cancel_gates(self) -> "QuantumCircuit":  # :189-216

@@ -33,6 +33,10 @@ struct qs_register {
     double* partials = nullptr;  // device: per-block reduction partials
     double* dres = nullptr;      // device: small results
     double* hres = nullptr;      // pinned host mirror of dres
+    // Qubits collapsed by measurements with no gate on them since: every amplitude whose zmask bits
+    // differ from zval is an exact zero, so later measurements visit only the live subspace.
+    uint64_t zmask = 0;
+    uint64_t zval = 0;
 };
 
 namespace qs {
@@ -170,6 +174,41 @@ namespace qs {
 void set_last_error_message(const std::string& msg) { g_last_error = msg; }
 }  // namespace qs
 
+namespace {
+
+// A gate maps the live subspace of the qubits it does not act on into itself (zero amplitudes there
+// stay exact zeros), so only its own targets leave the collapsed set. A matrix with a non-finite
+// entry can turn zeros into NaNs: then nothing is assumed any more.
+void touch_qubits(qs_register* reg, const double* matrix, const size_t* targets, size_t k) {
+    for (size_t j = 0; j < k; j++) {
+        const uint64_t b = 1ull << targets[j];
+        reg->zmask &= ~b;
+        reg->zval &= ~b;
+    }
+    const size_t entries = k < 32 ? (size_t(2) << (2 * k)) : 0;
+    for (size_t i = 0; i < entries; i++)
+        if (!std::isfinite(matrix[i])) {
+            reg->zmask = reg->zval = 0;
+            break;
+        }
+}
+
+// Reference-order (sequential) probability sums for complex128 registers in the exact arithmetic
+// up to this size; larger registers and the other forms use the parallel tree reduction.
+constexpr int kSequentialMaxQubits = 20;
+
+bool sequential_sums(const qs_register* reg) {
+    return reg->prec == QS_PREC_C128 && reg->arith == QS_ARITH_EXACT && reg->n <= kSequentialMaxQubits;
+}
+
+void record_outcome(qs_register* reg, size_t target, int res) {
+    const uint64_t b = 1ull << target;
+    reg->zmask |= b;
+    reg->zval = (reg->zval & ~b) | (res ? b : 0ull);
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* qs_last_error(void) { return g_last_error.c_str(); }
@@ -235,6 +274,8 @@ int qs_register_clone(const qs_register* src, qs_register** out) {
     int rc = allocate(size_t(src->n), src->prec, out);
     if (rc) return rc;
     (*out)->arith = src->arith;
+    (*out)->zmask = src->zmask;
+    (*out)->zval = src->zval;
     cudaError_t e = cudaStreamSynchronize(src->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync((*out)->state, src->state, (size_t(1) << src->n) * amp_bytes(src->prec),
@@ -255,7 +296,7 @@ int qs_register_precision(const qs_register* reg) { return reg ? reg->prec : -1;
 
 int qs_register_set_arith(qs_register* reg, int arith) {
     if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
-    if (arith != QS_ARITH_EXACT && arith != QS_ARITH_FMA && arith != QS_ARITH_DF64)
+    if (arith != QS_ARITH_EXACT && arith != QS_ARITH_FMA && arith != QS_ARITH_DF64 && arith != QS_ARITH_FX64)
         return set_err(QS_INVALID_ARGUMENT, "unknown arithmetic mode");
     reg->arith = arith;
     return QS_OK;
@@ -271,6 +312,7 @@ int qs_try_apply_fast(qs_register* reg, const double* matrix, size_t rows, size_
     if (!matrix) return set_err(QS_INVALID_ARGUMENT, "matrix is null");
     qs::OpDesc op;
     qs::classify_gate(matrix, k, targets, &op);
+    touch_qubits(reg, matrix, targets, k);
     rc = qs::apply_op(reg->state, reg->n, reg->prec, reg->arith, op, reg->stream, reg->sms, &msg);
     return rc ? set_err(rc, msg) : QS_OK;
 }
@@ -310,6 +352,19 @@ int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m, const qs_
         }
         qs::classify_gate(gates[g].matrix, gates[g].k, gates[g].targets, &ops[g]);
     }
+    for (size_t g = 0; g < m; g++) touch_qubits(reg, gates[g].matrix, gates[g].targets, gates[g].k);
+    if (o.fuse < 0 || o.fuse > 3) return set_err(QS_INVALID_ARGUMENT, "fuse must be 0..3");
+    const bool tune = o.fuse == 3 || (o.fuse == 1 && o.tile_qubits == 0) || (o.fuse == 2 && o.max_width == 0);
+    if (tune && qs::autotune_enabled()) {
+        qs::TuneReport rep;
+        int trc = qs::tune_circuit(reg->n, reg->prec, reg->arith, o.fuse, false, &rep, reg->sms, &msg);
+        if (trc) return set_err(trc, msg);
+        o.fuse = rep.best.fuse;
+        o.max_width = rep.best.width;
+        o.tile_qubits = rep.best.tile;
+    } else if (o.fuse == 3) {
+        o.fuse = 1;  // tuning switched off: stages at the automatic tile size
+    }
     int rc = qs::run_circuit(reg->state, reg->n, reg->prec, reg->arith, ops, gates, o, reg->stream, reg->sms, &msg);
     return rc ? set_err(rc, msg) : QS_OK;
 }
@@ -323,7 +378,7 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, d
         return set_err(QS_INVALID_TARGET, "InvalidTarget(" + std::to_string(target) + ")");
     }
     QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(target), reg->partials, kMaxPartials,
-                                     reg->dres, reg->stream, reg->sms),
+                                     reg->dres, reg->stream, reg->sms, reg->zmask, reg->zval, sequential_sums(reg)),
             "measure_probs");
     QS_CUDA(cudaMemcpyAsync(reg->hres, reg->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, reg->stream),
             "measure readback");
@@ -333,11 +388,65 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, d
     const double total = res ? p1 : p0;  // :323
     const double d = std::sqrt(total);
     const double rinv = 1.0 / d;
-    QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, int(target), res, d, rinv, reg->stream, reg->sms),
+    QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, int(target), res, d, rinv, reg->stream, reg->sms,
+                                reg->zmask, reg->zval),
             "collapse");
+    record_outcome(reg, target, res);
     if (outcome) *outcome = res;
     if (prob0) *prob0 = p0;
     if (prob1) *prob1 = p1;
+    return QS_OK;
+}
+
+int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
+                        double* prob0s, double* prob1s, size_t* err) {
+    qs::TraceRange trace("qs_measure_sequence");
+    if (!reg) return set_err(QS_INVALID_ARGUMENT, "register is null");
+    if (m && (!targets || !draws || !outcomes)) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    for (size_t k = 0; k < m; k++)
+        if (targets[k] >= size_t(reg->n)) {  // src/register.rs:299-301, checked before any work
+            if (err) {
+                err[0] = targets[k];
+                err[2] = k;
+            }
+            return set_err(QS_INVALID_TARGET, "InvalidTarget(" + std::to_string(targets[k]) + ")");
+        }
+    if (m == 0) return QS_OK;
+    const bool seq = sequential_sums(reg);
+    QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(targets[0]), reg->partials, kMaxPartials,
+                                     reg->dres, reg->stream, reg->sms, reg->zmask, reg->zval, seq),
+            "measure_probs");
+    for (size_t k = 0; k < m; k++) {
+        QS_CUDA(cudaMemcpyAsync(reg->hres, reg->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, reg->stream),
+                "measure readback");
+        QS_CUDA(cudaStreamSynchronize(reg->stream), "measure sync");
+        const double p0 = reg->hres[0], p1 = reg->hres[1];
+        const int res = draws[k] > p0 ? 1 : 0;
+        const double total = res ? p1 : p0;
+        const double d = std::sqrt(total);
+        const double rinv = 1.0 / d;
+        const int t = int(targets[k]);
+        if (k + 1 < m && !seq) {
+            QS_CUDA(qs::launch_collapse_probs(reg->state, reg->n, reg->prec, t, res, d, rinv, int(targets[k + 1]),
+                                              reg->partials, kMaxPartials, reg->dres, reg->stream, reg->sms,
+                                              reg->zmask, reg->zval),
+                    "collapse_probs");
+            record_outcome(reg, targets[k], res);
+        } else {
+            QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, t, res, d, rinv, reg->stream, reg->sms,
+                                        reg->zmask, reg->zval),
+                    "collapse");
+            record_outcome(reg, targets[k], res);
+            if (k + 1 < m)
+                QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(targets[k + 1]), reg->partials,
+                                                 kMaxPartials, reg->dres, reg->stream, reg->sms, reg->zmask,
+                                                 reg->zval, seq),
+                        "measure_probs");
+        }
+        outcomes[k] = res;
+        if (prob0s) prob0s[k] = p0;
+        if (prob1s) prob1s[k] = p1;
+    }
     return QS_OK;
 }
 
@@ -398,12 +507,42 @@ int qs_adjoint_gradient(qs_register* reg, const qs_param_gate* gates, size_t m, 
     if (reg->n < 1) return set_err(QS_INVALID_ARGUMENT, "register has no qubits");
     if (!terms_fit(terms, nterms, reg->n)) return set_err(QS_INVALID_ARGUMENT, "Pauli term acts on a qubit >= n");
     std::string msg;
+    reg->zmask = reg->zval = 0;  // the state is restored on return, but not assumed collapsed any more
     int rc = qs::adjoint_gradient(reg->state, reg->n, reg->prec, reg->arith, gates, m, params, nparams, terms, nterms,
                                   reg->stream, reg->sms, energy, grad, err, &msg);
     return rc ? set_err(rc, msg) : QS_OK;
 }
 
 uint64_t qs_launch_count(void) { return qs::g_launches.load(std::memory_order_relaxed); }
+
+int qs_circuit_autotune(size_t n, int precision, int arith, int fuse, int retune, qs_autotune_report* out) {
+    qs::TraceRange trace("qs_circuit_autotune");
+    if (!out) return set_err(QS_INVALID_ARGUMENT, "out is null");
+    std::memset(out, 0, sizeof(*out));
+    if (n < 1 || n > kMaxQubits) return set_err(QS_INVALID_ARGUMENT, "n out of range");
+    if (precision != QS_PREC_C128 && precision != QS_PREC_C64) return set_err(QS_INVALID_ARGUMENT, "unknown precision");
+    if (arith < QS_ARITH_EXACT || arith > QS_ARITH_FX64) return set_err(QS_INVALID_ARGUMENT, "unknown arithmetic mode");
+    if (fuse < 1 || fuse > 3) return set_err(QS_INVALID_ARGUMENT, "fuse must be 1, 2 or 3");
+    int dev = 0, sms = 1;
+    QS_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    QS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    qs::TuneReport rep;
+    std::string msg;
+    int rc = qs::tune_circuit(int(n), precision, arith, fuse, retune != 0, &rep, sms, &msg);
+    if (rc) return set_err(rc, msg);
+    out->fuse = rep.best.fuse;
+    out->max_width = rep.best.width;
+    out->tile_qubits = rep.best.tile;
+    out->from_cache = rep.from_cache ? 1 : 0;
+    out->count = int(std::min<size_t>(rep.cand.size(), QS_AUTOTUNE_MAX_CANDIDATES));
+    for (int i = 0; i < out->count; i++) {
+        out->cand_fuse[i] = rep.cand[i].fuse;
+        out->cand_width[i] = rep.cand[i].width;
+        out->cand_tile[i] = rep.cand[i].tile;
+        out->cand_ms[i] = rep.ms[i];
+    }
+    return QS_OK;
+}
 
 int qs_get_state(const qs_register* reg, double* dst) {
     qs::TraceRange trace("qs_get_state");
@@ -430,6 +569,7 @@ int qs_get_state(const qs_register* reg, double* dst) {
 int qs_set_state(qs_register* reg, const double* src) {
     qs::TraceRange trace("qs_set_state");
     if (!reg || !src) return set_err(QS_INVALID_ARGUMENT, "null argument");
+    reg->zmask = reg->zval = 0;
     const uint64_t N = 1ull << reg->n;
     if (reg->prec == QS_PREC_C128) {
         QS_CUDA(cudaMemcpyAsync(reg->state, src, N * 16, cudaMemcpyHostToDevice, reg->stream), "set_state");

@@ -1,0 +1,254 @@
+// qs_autotune.cpp — the autotune cache and the fusion autotuner of qs_apply_circuit.
+//
+// Which fusion form is fastest depends on the precision, the arithmetic and the register size:
+// complex64 register passes are issue-bound while 3xTF32 blocks trade FP32 work for tensor work;
+// complex128 double-float blocks pay off up to 3 qubits while FP64 blocks lose to single sweeps
+// (GB300 runs FP64 at 1/64 of the FP32 rate); the tile size trades shared-memory reuse against the
+// number of blocks sharing a mid-size state. The reference's counterpart is a caller choosing
+// QuantumCircuit reduction passes by hand (src/operation.rs:114-269; the timings in
+// examples/circuit_example.rs:24-28). Here candidates are timed once per (size, precision,
+// arithmetic, mode) on a scratch register running a seeded stand-in workload (two layers of
+// Haar-random 1-qubit gates on every qubit and CNOTs on a random perfect matching, the
+// benchmarks' circuit family) at min(n, 26) qubits, and the fastest is cached.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "qs_circuit.h"
+#include "qs_kernels.h"
+
+namespace qs {
+
+static std::string autotune_cache_path() {
+    if (const char* p = std::getenv("QS_AUTOTUNE_CACHE")) return p;
+    const char* home = std::getenv("HOME");
+    return home ? std::string(home) + "/.cache/quaru_gb300_autotune.txt" : std::string();
+}
+
+static std::mutex g_cache_mu;
+
+bool autotune_cache_lookup(const std::string& key, int* a, int* b) {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    const std::string p = autotune_cache_path();
+    if (p.empty()) return false;
+    std::ifstream f(p);
+    std::string k;
+    int x, y;
+    bool found = false;
+    while (f >> k >> x >> y)
+        if (k == key) {  // the last entry for a key wins (a re-tune appends)
+            *a = x;
+            *b = y;
+            found = true;
+        }
+    return found;
+}
+
+void autotune_cache_store(const std::string& key, int a, int b) {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    const std::string p = autotune_cache_path();
+    if (p.empty()) return;
+    std::ofstream f(p, std::ios::app);
+    if (f) f << key << " " << a << " " << b << "\n";
+}
+
+namespace {
+
+constexpr int kTuneMaxQubits = 26;
+constexpr int kTuneLayers = 2;
+
+uint64_t splitmix(uint64_t* s) {
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+double uniform(uint64_t* s) { return double(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+// The stand-in workload: per layer a random SU(2) element exp(i a) [[e^{ib} cos c, e^{id} sin c],
+// [-e^{-id} sin c, e^{-ib} cos c]] (dense complex, like a Haar-random gate) on every qubit, then
+// CNOTs on a random perfect matching.
+struct Workload {
+    std::vector<size_t> targets;
+    std::vector<double> mats;
+    std::vector<qs_gate> gates;
+    std::vector<OpDesc> ops;
+};
+
+void make_workload(int n, Workload* w) {
+    uint64_t s = 0x5EED7A7Eull + uint64_t(n);
+    struct G { size_t k; size_t t[2]; double m[32]; };
+    std::vector<G> list;
+    const double two_pi = 6.283185307179586;
+    for (int l = 0; l < kTuneLayers; l++) {
+        for (int q = 0; q < n; q++) {
+            const double a = two_pi * uniform(&s), b = two_pi * uniform(&s), c = two_pi * uniform(&s),
+                         d = two_pi * uniform(&s);
+            const double cc = std::cos(c), sc = std::sin(c);
+            auto ph = [&](double x, double r, double* out) {
+                out[0] = r * std::cos(x);
+                out[1] = r * std::sin(x);
+            };
+            G g{};
+            g.k = 1;
+            g.t[0] = size_t(q);
+            ph(a + b, cc, g.m + 0);
+            ph(a + d, sc, g.m + 2);
+            ph(a - d, -sc, g.m + 4);
+            ph(a - b, cc, g.m + 6);
+            list.push_back(g);
+        }
+        std::vector<int> p(n);
+        for (int i = 0; i < n; i++) p[i] = i;
+        for (int i = n - 1; i > 0; i--) std::swap(p[i], p[int(splitmix(&s) % uint64_t(i + 1))]);
+        for (int i = 0; i + 1 < n; i += 2) {
+            G g{};
+            g.k = 2;
+            g.t[0] = size_t(p[i + 1]);  // cnot(control, target): targets [target, control]
+            g.t[1] = size_t(p[i]);
+            const int on[4][2] = {{0, 0}, {1, 1}, {2, 3}, {3, 2}};
+            for (auto& e : on) g.m[2 * (4 * e[0] + e[1])] = 1.0;
+            list.push_back(g);
+        }
+    }
+    w->targets.clear();
+    w->mats.clear();
+    for (const G& g : list) {
+        for (size_t j = 0; j < g.k; j++) w->targets.push_back(g.t[j]);
+        for (size_t i = 0; i < (size_t(2) << (2 * g.k)); i++) w->mats.push_back(g.m[i]);
+    }
+    w->gates.resize(list.size());
+    w->ops.resize(list.size());
+    size_t to = 0, mo = 0;
+    for (size_t i = 0; i < list.size(); i++) {
+        w->gates[i].k = list[i].k;
+        w->gates[i].targets = w->targets.data() + to;
+        w->gates[i].matrix = w->mats.data() + mo;
+        classify_gate(w->gates[i].matrix, w->gates[i].k, w->gates[i].targets, &w->ops[i]);
+        to += list[i].k;
+        mo += size_t(2) << (2 * list[i].k);
+    }
+}
+
+std::string tune_key(int n, int prec, int arith, int mode) {
+    std::ostringstream k;
+    k << "circuit1:n" << n << ":p" << prec << ":a" << arith << ":m" << mode;
+    return k.str();
+}
+
+std::mutex g_memo_mu;
+std::map<std::string, TuneChoice> g_memo;
+
+}  // namespace
+
+bool autotune_enabled() {
+    const char* v = std::getenv("QS_AUTOTUNE");
+    return !(v && (std::strcmp(v, "off") == 0 || std::strcmp(v, "0") == 0));
+}
+
+std::vector<TuneChoice> tune_candidates(int n, int prec, int mode) {
+    std::vector<TuneChoice> c;
+    const int m = std::min(n, kTuneMaxQubits);
+    if (mode == 3) c.push_back({0, 0, 0});
+    if (mode == 1 || mode == 3) {
+        const int lo = prec == QS_PREC_C64 ? 9 : 8, hi = prec == QS_PREC_C64 ? 12 : 11;
+        for (int T = lo; T <= std::min(hi, m); T++) c.push_back({1, 0, T});
+        if (c.empty() || c.back().fuse != 1) c.push_back({1, 0, 0});  // tiny registers: the automatic tile
+    }
+    if (mode == 2 || mode == 3)
+        for (int W = 2; W <= 5; W++) c.push_back({2, W, 0});
+    return c;
+}
+
+int tune_circuit(int n, int prec, int arith, int mode, bool retune, TuneReport* rep, int sms, std::string* msg) {
+    rep->cand.clear();
+    rep->ms.clear();
+    rep->from_cache = false;
+    const std::string key = tune_key(n, prec, arith, mode);
+    if (!retune) {
+        {
+            std::lock_guard<std::mutex> lock(g_memo_mu);
+            auto it = g_memo.find(key);
+            if (it != g_memo.end()) {
+                rep->best = it->second;
+                rep->from_cache = true;
+                return QS_OK;
+            }
+        }
+        int a = 0, b = 0;
+        if (autotune_cache_lookup(key, &a, &b)) {
+            rep->best = TuneChoice{a >> 4, a & 15, b};
+            rep->from_cache = true;
+            std::lock_guard<std::mutex> lock(g_memo_mu);
+            g_memo[key] = rep->best;
+            return QS_OK;
+        }
+    }
+    const int m = std::min(n, kTuneMaxQubits);
+    Workload w;
+    make_workload(m, &w);
+    const size_t amp = prec == QS_PREC_C64 ? 8 : 16;
+    cudaStream_t s = nullptr;
+    void* scratch = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocAsync(&scratch, (size_t(1) << m) * amp, s);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = launch_init_basis(scratch, m, prec, 0, s, sms);
+    int rc = QS_OK;
+    if (e == cudaSuccess) {
+        qs_circuit_options o0;
+        std::memset(&o0, 0, sizeof(o0));
+        rc = run_circuit(scratch, m, prec, arith, w.ops, w.gates.data(), o0, s, sms, msg);  // a dense state
+    }
+    double best = 1e300;
+    TuneChoice bestc{1, 0, 0};
+    for (const TuneChoice& c : tune_candidates(n, prec, mode)) {
+        if (e != cudaSuccess || rc != QS_OK) break;
+        qs_circuit_options o;
+        std::memset(&o, 0, sizeof(o));
+        o.fuse = c.fuse;
+        o.max_width = c.width;
+        o.tile_qubits = c.tile;
+        rc = run_circuit(scratch, m, prec, arith, w.ops, w.gates.data(), o, s, sms, msg);  // warm-up
+        if (rc != QS_OK) break;
+        e = cudaEventRecord(e0, s);
+        if (e == cudaSuccess) rc = run_circuit(scratch, m, prec, arith, w.ops, w.gates.data(), o, s, sms, msg);
+        if (e == cudaSuccess && rc == QS_OK) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess && rc == QS_OK) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess && rc == QS_OK) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess || rc != QS_OK) break;
+        rep->cand.push_back(c);
+        rep->ms.push_back(double(ms));
+        if (ms < best) best = ms, bestc = c;
+    }
+    if (scratch) cudaFreeAsync(scratch, s);
+    if (s) cudaStreamSynchronize(s);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    if (rc != QS_OK) return rc;
+    if (e != cudaSuccess) {
+        if (msg) *msg = std::string("autotune: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? QS_OUT_OF_MEMORY : QS_CUDA_ERROR;
+    }
+    rep->best = bestc;
+    autotune_cache_store(key, (bestc.fuse << 4) | bestc.width, bestc.tile);
+    std::lock_guard<std::mutex> lock(g_memo_mu);
+    g_memo[key] = bestc;
+    return QS_OK;
+}
+
+}  // namespace qs

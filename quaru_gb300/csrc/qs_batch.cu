@@ -576,34 +576,6 @@ cudaError_t capture(qs_batch* b) {
     return cudaGraphInstantiate(&b->exec, b->graph, 0);
 }
 
-std::string cache_path() {
-    if (const char* p = std::getenv("QS_AUTOTUNE_CACHE")) return p;
-    const char* home = std::getenv("HOME");
-    return home ? std::string(home) + "/.cache/quaru_gb300_autotune.txt" : std::string();
-}
-
-bool cache_lookup(const std::string& key, int* cl, int* ct) {
-    const std::string p = cache_path();
-    if (p.empty()) return false;
-    std::ifstream f(p);
-    std::string k;
-    int a, b;
-    while (f >> k >> a >> b)
-        if (k == key) {
-            *cl = a;
-            *ct = b;
-            return true;
-        }
-    return false;
-}
-
-void cache_store(const std::string& key, int cl, int ct) {
-    const std::string p = cache_path();
-    if (p.empty()) return;
-    std::ofstream f(p, std::ios::app);
-    if (f) f << key << " " << cl << " " << ct << "\n";
-}
-
 // Planning form of one gate (targets forced into the tile, controls free): rotations and fixed
 // 1-qubit gates as dense 1-qubit gates on their target, CNOT as classified (target + control).
 OpDesc plan_desc(const qs_param_gate& G, bool cnot) {
@@ -896,7 +868,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
     int cl = o.chunk_log2, ct = o.ctas_per_sm;
     if (cl <= 0 || ct <= 0) {
         int ccl = 0, cct = 0;
-        if (cache_lookup(key.str(), &ccl, &cct)) {
+        if (autotune_cache_lookup(key.str(), &ccl, &cct)) {
             if (cl <= 0) cl = ccl;
             if (ct <= 0) ct = cct;
         }
@@ -929,7 +901,7 @@ extern "C" int qs_batch_create(const qs_batch_circuit* circuits, size_t count, c
         }
         cl = bcl;
         ct = bct;
-        if (e == cudaSuccess) cache_store(key.str(), cl, ct);
+        if (e == cudaSuccess) autotune_cache_store(key.str(), cl, ct);
     }
     b->ctas = std::max(1, std::min(ct, max_per_sm));
     if (e == cudaSuccess) e = layout(std::max(kMinChunk, cl));

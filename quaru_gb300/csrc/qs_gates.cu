@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -40,7 +41,7 @@ struct Dense1Args {
 // x1.im = 0..3) number t for real outputs and t ^ 1 for imaginary outputs.
 
 // MODE 0: exact complex, 1: exact real, 2: FMA complex, 3: FMA real,
-// 4: double-float complex, 5: double-float real (complex128 only).
+// 4: double-float complex, 5: double-float real (4-5: complex128 only).
 template <typename R, int MODE, int ILP>
 __global__ void __launch_bounds__(kThreads) k_dense1(typename Cplx<R>::T* __restrict__ st, uint64_t ntup,
                                                      const __grid_constant__ Dense1Args<R> a) {
@@ -114,6 +115,96 @@ __global__ void __launch_bounds__(kThreads) k_dense1(typename Cplx<R>::T* __rest
             st[i0[u]] = y0;
             st[i0[u] | a.tbit] = y1;
         }
+    }
+}
+
+// ---------------------------------------------------------------- 1-qubit dense, fixed point
+// QS_ARITH_FX64 (see fx_encode in qs_device.cuh): each output component of a pair is an integer dot
+// product rounded once to double. Outputs o = (y0.re, y0.im, y1.re, y1.im), terms t over
+// (x0.re, x0.im, x1.re, x1.im); a real matrix uses terms (o & 1) and 2 + (o & 1) only.
+struct Dense1FxArgs {
+    IndexMap map;       // tuple expansion (gates with fixed bits)
+    uint64_t tbit;      // 1 << target
+    int32_t fxh[16];    // row o, term t: 30-bit limbs of C = RN(c * 2^(60 - ec))
+    int32_t fxl[16];
+    int32_t fxk[4];     // ec - 1082 per output
+    int32_t fxkk[4];    // (ec - 1082) << 20
+    int32_t kmin, kmax; // range of fxk over the outputs
+    double m[8];        // the matrix, for tuples with infinite or NaN components (FP64 FMA)
+};
+
+// Every tuple the fast path does not take: infinite or NaN components (FP64 FMA propagates them),
+// components all below 2^-958, or output exponents near the ends of the double range.
+template <bool REAL>
+__device__ __noinline__ void fx_pair_slow(double2 x0, double2 x1, const Dense1FxArgs& a, double2* y0, double2* y1) {
+    const double v[4] = {x0.x, x0.y, x1.x, x1.y};
+    const uint32_t E = max(max(fx_efield(v[0]), fx_efield(v[1])), max(fx_efield(v[2]), fx_efield(v[3])));
+    if (E == 0x7ffu) {
+        *y0 = cfma(a.m[0], a.m[1], x0, cfma(a.m[2], a.m[3], x1, czero<double2>()));
+        *y1 = cfma(a.m[4], a.m[5], x0, cfma(a.m[6], a.m[7], x1, czero<double2>()));
+        return;
+    }
+    int32_t vh[4], vl[4];
+    for (int t = 0; t < 4; t++) {
+        if (E >= kFxMinE)
+            fx_encode(v[t], E, vh[t], vl[t]);
+        else
+            fx_encode_small(v[t], E, vh[t], vl[t]);
+    }
+    double out[4];
+    for (int o = 0; o < 4; o++) {
+        if (REAL) {
+            const int32_t th[2] = {vh[o & 1], vh[2 + (o & 1)]}, tl[2] = {vl[o & 1], vl[2 + (o & 1)]};
+            const int32_t ch[2] = {a.fxh[4 * o + (o & 1)], a.fxh[4 * o + 2 + (o & 1)]};
+            const int32_t cl[2] = {a.fxl[4 * o + (o & 1)], a.fxl[4 * o + 2 + (o & 1)]};
+            out[o] = fx_dot<2>(th, tl, ch, cl, E, a.fxk[o]);
+        } else {
+            out[o] = fx_dot<4>(vh, vl, a.fxh + 4 * o, a.fxl + 4 * o, E, a.fxk[o]);
+        }
+    }
+    *y0 = make_double2(out[0], out[1]);
+    *y1 = make_double2(out[2], out[3]);
+}
+
+// PLAIN: the gate has no fixed bits, so a tuple index expands by one inserted bit.
+template <bool REAL, bool PLAIN>
+__global__ void __launch_bounds__(kThreads, 6) k_dense1_fx(double2* __restrict__ st, uint64_t ntup,
+                                                        const __grid_constant__ Dense1FxArgs a) {
+    const uint64_t stride = uint64_t(gridDim.x) * kThreads;
+    const uint64_t lo_mask = a.tbit - 1ull;
+    for (uint64_t t = uint64_t(blockIdx.x) * kThreads + threadIdx.x; t < ntup; t += stride) {
+        const uint64_t i0 = PLAIN ? (((t & ~lo_mask) << 1) | (t & lo_mask)) : expand_index(t, a.map);
+        const double2 x0 = st[i0], x1 = st[i0 | a.tbit];
+        double2 y0, y1;
+        const uint32_t E = max(max(fx_efield(x0.x), fx_efield(x0.y)), max(fx_efield(x1.x), fx_efield(x1.y)));
+        if (E >= kFxMinE && E < 0x7ffu && int(E) + a.kmin >= kFxFastKMin && int(E) + a.kmax <= kFxFastKMax) {
+            int32_t vh[4], vl[4];
+            fx_encode(x0.x, E, vh[0], vl[0]);
+            fx_encode(x0.y, E, vh[1], vl[1]);
+            fx_encode(x1.x, E, vh[2], vl[2]);
+            fx_encode(x1.y, E, vh[3], vl[3]);
+            const int ek = int(E << 20);
+            double out[4];
+#pragma unroll
+            for (int o = 0; o < 4; o++) {
+                long long R;
+                if constexpr (REAL) {
+                    const int32_t th[2] = {vh[o & 1], vh[2 + (o & 1)]}, tl[2] = {vl[o & 1], vl[2 + (o & 1)]};
+                    const int32_t ch[2] = {a.fxh[4 * o + (o & 1)], a.fxh[4 * o + 2 + (o & 1)]};
+                    const int32_t cl[2] = {a.fxl[4 * o + (o & 1)], a.fxl[4 * o + 2 + (o & 1)]};
+                    R = fx_row_sum<2>(th, tl, ch, cl);
+                } else {
+                    R = fx_row_sum<4>(vh, vl, a.fxh + 4 * o, a.fxl + 4 * o);
+                }
+                out[o] = fx_to_double_fast(R, int(uint32_t(ek) + uint32_t(a.fxkk[o])));
+            }
+            y0 = make_double2(out[0], out[1]);
+            y1 = make_double2(out[2], out[3]);
+        } else {
+            fx_pair_slow<REAL>(x0, x1, a, &y0, &y1);
+        }
+        st[i0] = y0;
+        st[i0 | a.tbit] = y1;
     }
 }
 
@@ -366,9 +457,54 @@ static bool fill_df64(Dense1Args<R>& a) {
     return true;
 }
 
+// Fixed-point coefficients of one output row (QS_ARITH_FX64): C_t = RN(c_t * 2^(60 - ec)) split into
+// 30-bit limbs, ec the frexp exponent of the row's largest |c_t|; k0 = ec - 1082. False for
+// non-finite entries (the FP64 kernel runs instead).
+static bool fx_row(const double* c, int nt, int32_t* h, int32_t* l, int32_t* k0) {
+    double cmax = 0.0;
+    for (int t = 0; t < nt; t++) {
+        if (!std::isfinite(c[t])) return false;
+        cmax = std::max(cmax, std::fabs(c[t]));
+    }
+    int ec = 0;
+    if (cmax > 0.0) std::frexp(cmax, &ec);
+    for (int t = 0; t < nt; t++) {
+        const long long C = std::llrint(std::ldexp(c[t], 60 - ec));  // |C| < 2^60
+        const long long lo = (long long)((unsigned long long)C << 34) >> 34;  // low 30 bits, balanced
+        h[t] = int32_t((C - lo) >> 30);
+        l[t] = int32_t(lo);
+    }
+    *k0 = ec - 1082;
+    return true;
+}
+
+// The coefficients of k_dense1_fx: output o = (y0.re, y0.im, y1.re, y1.im), term t over
+// (x0.re, x0.im, x1.re, x1.im). False for non-finite entries (the FP64 kernel runs instead).
+static bool fill_fx(const OpDesc& op, Dense1FxArgs& a) {
+    for (int i = 0; i < 8; i++) a.m[i] = op.m[i];
+    a.kmin = 1 << 30;
+    a.kmax = -(1 << 30);
+    for (int o = 0; o < 4; o++) {
+        const int row = o >> 1;
+        const double ar = op.m[4 * row], ai = op.m[4 * row + 1];      // u[row][0]
+        const double br = op.m[4 * row + 2], bi = op.m[4 * row + 3];  // u[row][1]
+        double c[4];
+        if ((o & 1) == 0) {  // re = ar x0r - ai x0i + br x1r - bi x1i
+            c[0] = ar; c[1] = -ai; c[2] = br; c[3] = -bi;
+        } else {             // im = ai x0r + ar x0i + bi x1r + br x1i
+            c[0] = ai; c[1] = ar; c[2] = bi; c[3] = br;
+        }
+        if (!fx_row(c, 4, a.fxh + 4 * o, a.fxl + 4 * o, a.fxk + o)) return false;
+        a.fxkk[o] = int32_t(uint32_t(a.fxk[o]) << 20);
+        a.kmin = std::min(a.kmin, a.fxk[o]);
+        a.kmax = std::max(a.kmax, a.fxk[o]);
+    }
+    return true;
+}
+
 template <typename R>
 static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms,
-                                 bool df64 = false) {
+                                 bool df64 = false, bool fx64 = false) {
     using T = typename Cplx<R>::T;
     Dense1Args<R> a;
     std::memset(&a, 0, sizeof(a));
@@ -387,6 +523,27 @@ static cudaError_t launch_dense1(const OpDesc& op, void* state, int n, bool exac
             else
                 k_dense1<R, 0, ILP><<<grid, kThreads, 0, s>>>(st, ntup, a);
             return counted(cudaGetLastError());
+        }
+        if (fx64) {
+            Dense1FxArgs f;
+            std::memset(&f, 0, sizeof(f));
+            if (fill_fx(op, f)) {
+                f.map = a.map;
+                f.tbit = a.tbit;
+                // one pair per thread: the integer form needs few registers, so 64 warps fit per SM
+                const int g1 = grid_for(ntup, sms, 1);
+                double2* sd = reinterpret_cast<double2*>(state);
+                const bool plain = op.fixmask == 0;
+                if (real && plain)
+                    k_dense1_fx<true, true><<<g1, kThreads, 0, s>>>(sd, ntup, f);
+                else if (real)
+                    k_dense1_fx<true, false><<<g1, kThreads, 0, s>>>(sd, ntup, f);
+                else if (plain)
+                    k_dense1_fx<false, true><<<g1, kThreads, 0, s>>>(sd, ntup, f);
+                else
+                    k_dense1_fx<false, false><<<g1, kThreads, 0, s>>>(sd, ntup, f);
+                return counted(cudaGetLastError());
+            }
         }
         if (df64 && fill_df64(a)) {
             if (real)
@@ -530,7 +687,7 @@ static cudaError_t launch_mono(const OpDesc& op, void* state, int n, cudaStream_
 
 template <typename R>
 static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact, cudaStream_t s, int sms,
-                                bool df64 = false) {
+                                bool df64 = false, bool fx64 = false) {
     if (op.kind == OP_MONO || op.kind == OP_MONO_PF) {
         switch (op.k) {
             case 0: return launch_mono<R, 0>(op, state, n, s, sms);
@@ -553,7 +710,7 @@ static cudaError_t launch_small(const OpDesc& op, void* state, int n, bool exact
                 z.pf[0] = 255;
                 return launch_mono<R, 0>(z, state, n, s, sms);
             }
-            case 1: return launch_dense1<R>(op, state, n, exact, s, sms, df64);
+            case 1: return launch_dense1<R>(op, state, n, exact, s, sms, df64, fx64);
             case 2: return launch_denseK<R, 2>(op, state, n, exact, s, sms, df64);
             case 3: return launch_denseK<R, 3>(op, state, n, exact, s, sms, df64);
             case 4: return launch_denseK<R, 4>(op, state, n, exact, s, sms);
@@ -568,7 +725,7 @@ cudaError_t launch_op(const OpDesc& op, void* state, int n, int prec, int arith,
     if (op.k > kMaxSmallK) return cudaErrorInvalidValue;
     const bool exact = (arith == QS_ARITH_EXACT);
     if (prec == QS_PREC_C64) return launch_small<float>(op, state, n, false, s, sms);
-    return launch_small<double>(op, state, n, exact, s, sms, arith == QS_ARITH_DF64);
+    return launch_small<double>(op, state, n, exact, s, sms, arith == QS_ARITH_DF64, arith == QS_ARITH_FX64);
 }
 
 cudaError_t launch_op_big(const OpDesc& op, void* state, const void* src, int n, int prec, int arith,

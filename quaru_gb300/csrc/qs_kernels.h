@@ -41,6 +41,11 @@ void* pinned_staging(int slot, size_t bytes);
 // Set the message qs_last_error() returns on the calling thread.
 void set_last_error_message(const std::string& msg);
 
+// The autotune cache: one line "key a b" per tuned configuration, in QS_AUTOTUNE_CACHE or
+// ~/.cache/quaru_gb300_autotune.txt; shared by the batch and circuit tuners (qs_autotune.cpp).
+bool autotune_cache_lookup(const std::string& key, int* a, int* b);
+void autotune_cache_store(const std::string& key, int a, int b);
+
 // Device tables of a sub-operation wider than kMaxSmallK qubits.
 struct BigOpBuffers {
     const uint64_t* off = nullptr;
@@ -64,12 +69,21 @@ void big_op_host_tables(const OpDesc& op, int prec, std::vector<uint64_t>* off, 
 // ---- state-wide kernels (qs_state.cu) ----
 cudaError_t launch_init_basis(void* state, int n, int prec, uint64_t index, cudaStream_t s, int sms);
 cudaError_t launch_init_product(void* state, int n, int prec, const double* qubits, cudaStream_t s, int sms);
-// FP64 probability sums of target bit 0 / 1 into out[0], out[1] (device), via per-block partials.
+// FP64 probability sums of target bit 0 / 1 into out[0], out[1] (device), via per-block partials,
+// over the live subspace (amplitudes whose zmask bits equal zval; the others must be zero).
+// sequential (complex128 only): one block adds the squares in index order, as the reference does.
 cudaError_t launch_measure_probs(const void* state, int n, int prec, int target, double* partials,
-                                 int max_partials, double* out, cudaStream_t s, int sms);
-// Zero amplitudes whose target bit != outcome and divide the rest by d (rinv = 1/d).
+                                 int max_partials, double* out, cudaStream_t s, int sms, uint64_t zmask = 0,
+                                 uint64_t zval = 0, bool sequential = false);
+// Zero amplitudes whose target bit != outcome and divide the rest by d (rinv = 1/d), within the
+// live subspace.
 cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
-                            cudaStream_t s, int sms);
+                            cudaStream_t s, int sms, uint64_t zmask = 0, uint64_t zval = 0);
+// The same collapse, with the probability sums of next_target over the kept amplitudes written to
+// out[0], out[1] (device) in the same pass.
+cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int outcome, double d, double rinv,
+                                  int next_target, double* partials, int max_partials, double* out, cudaStream_t s,
+                                  int sms, uint64_t zmask, uint64_t zval);
 // norm_sqr of amplitudes [first, first + count) into dst (device).
 cudaError_t launch_norm_sqr(const void* state, int prec, uint64_t first, uint64_t count, double* dst,
                             cudaStream_t s, int sms);

@@ -111,7 +111,10 @@ int na_err(int code, const std::string& msg) {
 }
 
 // Set-up, once per device, with that device current: the host-side name of
-// g_noalloc_partials is only a stand-in, so look up its device address.
+// g_noalloc_partials is only a stand-in, so look up its device address. The
+// address is kept for the life of the process; cudaDeviceReset (or any other
+// teardown of the device's primary context) unloads the module and makes it
+// stale, so callers do not reset a device they keep using this entry point on.
 int scratch_for_current_device(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -137,6 +140,11 @@ extern "C" int qs_measure_probabilities_noalloc(const void* state, size_t n, int
     using namespace qs;
     if (!state || !out) return na_err(QS_INVALID_ARGUMENT, "state and out must be device pointers");
     if (precision != QS_PREC_C128 && precision != QS_PREC_C64) return na_err(QS_INVALID_ARGUMENT, "unknown precision");
+    // The kernels load whole amplitudes (16 or 8 bytes) and store doubles: a misaligned pointer
+    // would fault on the GPU and end the caller's context, so it is refused here instead.
+    const uintptr_t amp_align = precision == QS_PREC_C128 ? 16 : 8;
+    if (reinterpret_cast<uintptr_t>(state) % amp_align != 0 || reinterpret_cast<uintptr_t>(out) % 8 != 0)
+        return na_err(QS_INVALID_ARGUMENT, "state must be aligned to its amplitude size and out to 8 bytes");
     if (n < 1 || n > 40) return na_err(QS_INVALID_ARGUMENT, "n must be in 1..40");
     if (target >= n) {
         if (err) err[0] = target;

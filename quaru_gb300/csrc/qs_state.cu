@@ -34,7 +34,7 @@ __device__ __forceinline__ double2 to_d2(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d2(float2 v) { return make_double2(double(v.x), double(v.y)); }
 // Reductions and the collapse read complex64 amplitudes through an integer-pipe conversion: the FP64
 // pipe (~1/64 of the FP32 rate on GB300) is left to the sums and quotients themselves. Exact for
-// normal floats; subnormal floats (< 2^-126) read as zero, far below every tolerance they feed.
+// every float (subnormals take a rare branch), so the values equal double(v).
 __device__ __forceinline__ double2 to_d2_int(double2 v) { return v; }
 __device__ __forceinline__ double2 to_d2_int(float2 v) { return make_double2(df_f2d(v.x), df_f2d(v.y)); }
 __device__ __forceinline__ void from_d2(double2* dst, double2 v) { *dst = v; }
@@ -149,14 +149,35 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
     }
 }
 
+// A measurement visits the pairs (i0, i0 | tb) of its target inside the register's live subspace:
+// amplitudes whose collapsed qubits (earlier measurements, no gate on them since) differ from the
+// recorded outcomes are exact zeros, so they add nothing to a probability sum and a collapse leaves
+// them as they are. The pair index t expands to i0 with the target bit 0 and the collapsed bits at
+// their values.
+static IndexMap subspace_map(int target, uint64_t zmask, uint64_t zval) {
+    IndexMap m;
+    std::memset(&m, 0, sizeof(m));
+    const uint64_t pos = (zmask & ~(1ull << target)) | (1ull << target);
+    int k = 0;
+    for (int b = 0; b < 64; b++)
+        if (pos >> b & 1ull) m.pos[k++] = uint8_t(b);
+    m.npos = k;
+    m.fixval = zval & zmask & ~(1ull << target);
+    return m;
+}
+
+static uint64_t subspace_pairs(int n, int target, uint64_t zmask) {
+    return 1ull << (n - 1 - __builtin_popcountll(zmask & ~(1ull << target)));
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kT) k_prob_partials(const T* __restrict__ st, uint64_t npairs, int target,
+__global__ void __launch_bounds__(kT) k_prob_partials(const T* __restrict__ st, uint64_t npairs, uint64_t tb,
+                                                      const __grid_constant__ IndexMap map,
                                                       double* __restrict__ partials) {
-    const uint64_t lo_mask = (1ull << target) - 1ull, tb = 1ull << target;
     const uint64_t stride = uint64_t(gridDim.x) * kT;
     double p0 = 0.0, p1 = 0.0;
     for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
-        const uint64_t i0 = ((t & ~lo_mask) << 1) | (t & lo_mask);
+        const uint64_t i0 = expand_index(t, map);
         const double2 a = to_d2_int(st[i0]);
         const double2 b = to_d2_int(st[i0 | tb]);
         p0 = fma(a.x, a.x, p0);
@@ -185,15 +206,64 @@ __global__ void __launch_bounds__(kT) k_prob_final(const double* __restrict__ pa
     }
 }
 
+// The probability sums in the reference's order (src/register.rs:306-315): norm_sqr = re*re + im*im
+// rounded per operation, added to prob_0 or prob_1 one amplitude after another in index order. One
+// block stages chunks of amplitudes in shared memory; the bit-0 and bit-1 chains are independent
+// sums and run on two threads. Amplitudes outside the live subspace are exact zeros, which leave a
+// running sum unchanged, so only the subspace is read.
+constexpr int kSeqChunk = 2048;
+__global__ void __launch_bounds__(kT) k_prob_sequential(const double2* __restrict__ st, uint64_t count, int target,
+                                                        const __grid_constant__ IndexMap map,
+                                                        double* __restrict__ out) {
+    __shared__ double pr[kSeqChunk];
+    __shared__ uint8_t bit[kSeqChunk];
+    double acc = 0.0;  // thread 0: prob_0, thread 32: prob_1
+    for (uint64_t base = 0; base < count; base += kSeqChunk) {
+        const int len = int(count - base < uint64_t(kSeqChunk) ? count - base : uint64_t(kSeqChunk));
+        for (int j = threadIdx.x; j < len; j += kT) {
+            const uint64_t i = expand_index(base + uint64_t(j), map);
+            const double2 a = st[i];
+            pr[j] = __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
+            bit[j] = uint8_t((i >> target) & 1ull);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 || threadIdx.x == 32) {
+            const uint8_t want = threadIdx.x == 32 ? 1 : 0;
+            for (int j = 0; j < len; j++)
+                if (bit[j] == want) acc = __dadd_rn(acc, pr[j]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = acc;
+    if (threadIdx.x == 32) out[1] = acc;
+}
+
 cudaError_t launch_measure_probs(const void* state, int n, int prec, int target, double* partials,
-                                 int max_partials, double* out, cudaStream_t s, int sms) {
-    const uint64_t npairs = 1ull << (n - 1);
+                                 int max_partials, double* out, cudaStream_t s, int sms, uint64_t zmask,
+                                 uint64_t zval, bool sequential) {
+    const IndexMap map = subspace_map(target, zmask, zval);
+    const uint64_t npairs = subspace_pairs(n, target, zmask);
+    const uint64_t tb = 1ull << target;
+    if (sequential && prec == QS_PREC_C128) {
+        // every amplitude of the subspace in index order: the free bits are all bits but the
+        // collapsed ones (the target's bit is free here)
+        IndexMap all;
+        std::memset(&all, 0, sizeof(all));
+        int k = 0;
+        const uint64_t fixed = zmask & ~tb;
+        for (int b = 0; b < 64; b++)
+            if (fixed >> b & 1ull) all.pos[k++] = uint8_t(b);
+        all.npos = k;
+        all.fixval = zval & fixed;
+        k_prob_sequential<<<1, kT, 0, s>>>((const double2*)state, 2 * npairs, target, all, out);
+        return counted(cudaGetLastError());
+    }
     int grid = grid_cap(npairs, sms, 4);
     if (grid > max_partials) grid = max_partials;
     if (prec == QS_PREC_C64)
-        k_prob_partials<float2><<<grid, kT, 0, s>>>((const float2*)state, npairs, target, partials);
+        k_prob_partials<float2><<<grid, kT, 0, s>>>((const float2*)state, npairs, tb, map, partials);
     else
-        k_prob_partials<double2><<<grid, kT, 0, s>>>((const double2*)state, npairs, target, partials);
+        k_prob_partials<double2><<<grid, kT, 0, s>>>((const double2*)state, npairs, tb, map, partials);
     k_prob_final<<<1, kT, 0, s>>>(partials, grid, out);
     return counted(cudaGetLastError(), 2);
 }
@@ -208,24 +278,19 @@ __device__ __forceinline__ double div_markstein(double x, double d, double rinv)
     return fma(r, rinv, q);
 }
 
+// The kept amplitude divided by sqrt(total) (src/register.rs:337), in the state's type.
 template <typename T, bool TRUEDIV>
-__global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t npairs, int target, int outcome,
-                                                 double d, double rinv) {
-    const uint64_t lo_mask = (1ull << target) - 1ull, tb = 1ull << target;
-    const uint64_t stride = uint64_t(gridDim.x) * kT;
-    for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
-        const uint64_t i0 = ((t & ~lo_mask) << 1) | (t & lo_mask);
-        const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
-        if constexpr (sizeof(T) == 8 && !TRUEDIV) {
-            // complex64: one FP64 multiply by RN(1/d) per component, rounded to float on the
-            // integer pipe (the quotient is stored as a float, so the exactly rounded double
-            // quotient of the complex128 path buys nothing here)
-            const double2 x = to_d2_int(st[keep]);
-            st[keep] = T{d2f_int(x.x * rinv), d2f_int(x.y * rinv)};
-            st[drop] = T{0.0f, 0.0f};
-            continue;
-        }
-        const double2 x = to_d2_int(st[keep]);
+__device__ __forceinline__ T collapse_value(T v, double d, double rinv, double2* as_double) {
+    if constexpr (sizeof(T) == 8 && !TRUEDIV) {
+        // complex64: one FP64 multiply by RN(1/d) per component, rounded to float on the integer
+        // pipe (the quotient is stored as a float, so the exactly rounded double quotient of the
+        // complex128 path buys nothing here)
+        const double2 x = to_d2_int(v);
+        const T y{d2f_int(x.x * rinv), d2f_int(x.y * rinv)};
+        *as_double = make_double2(df_f2d(y.x), df_f2d(y.y));
+        return y;
+    } else {
+        const double2 x = to_d2_int(v);
         double2 y;
         if (TRUEDIV) {
             y.x = x.x / d;
@@ -234,29 +299,107 @@ __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t np
             y.x = div_markstein(x.x, d, rinv);
             y.y = div_markstein(x.y, d, rinv);
         }
-        from_d2(&st[keep], y);
-        from_d2(&st[drop], make_double2(0.0, 0.0));
+        T r;
+        from_d2(&r, y);
+        *as_double = to_d2_int(r);
+        return r;
     }
 }
 
-cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
-                            cudaStream_t s, int sms) {
-    const uint64_t npairs = 1ull << (n - 1);
-    const int grid = grid_cap(npairs, sms, 2);
+template <typename T, bool TRUEDIV>
+__global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t npairs, uint64_t tb,
+                                                 const __grid_constant__ IndexMap map, int outcome, double d,
+                                                 double rinv) {
+    const uint64_t stride = uint64_t(gridDim.x) * kT;
+    for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
+        const uint64_t i0 = expand_index(t, map);
+        const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
+        double2 unused;
+        st[keep] = collapse_value<T, TRUEDIV>(st[keep], d, rinv, &unused);
+        st[drop] = T{0, 0};
+    }
+}
+
+// The collapse of one measurement fused with the probability sums of the next one (measure_circuit,
+// src/register.rs:371-377): the kept amplitudes, once divided, are the only non-zero amplitudes the
+// next target sees, so their squares are summed by that target's bit in the same pass.
+template <typename T, bool TRUEDIV>
+__global__ void __launch_bounds__(kT) k_collapse_probs(T* __restrict__ st, uint64_t npairs, uint64_t tb,
+                                                       const __grid_constant__ IndexMap map, int outcome, double d,
+                                                       double rinv, uint64_t next_tb, double* __restrict__ partials) {
+    const uint64_t stride = uint64_t(gridDim.x) * kT;
+    double p0 = 0.0, p1 = 0.0;
+    for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
+        const uint64_t i0 = expand_index(t, map);
+        const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
+        double2 y;
+        st[keep] = collapse_value<T, TRUEDIV>(st[keep], d, rinv, &y);
+        st[drop] = T{0, 0};
+        const double q = fma(y.x, y.x, y.y * y.y);
+        if (keep & next_tb)
+            p1 += q;
+        else
+            p0 += q;
+    }
+    block_sum2(p0, p1);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = p0;
+        partials[2 * blockIdx.x + 1] = p1;
+    }
+}
+
+static bool use_truediv(double d, double rinv) {
     // Markstein's step needs a finite reciprocal of a normal divisor.
-    const bool truediv = !(std::isfinite(rinv) && d > 1e-300 && std::isfinite(d));
+    return !(std::isfinite(rinv) && d > 1e-300 && std::isfinite(d));
+}
+
+cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
+                            cudaStream_t s, int sms, uint64_t zmask, uint64_t zval) {
+    const IndexMap map = subspace_map(target, zmask, zval);
+    const uint64_t npairs = subspace_pairs(n, target, zmask);
+    const uint64_t tb = 1ull << target;
+    const int grid = grid_cap(npairs, sms, 2);
+    const bool truediv = use_truediv(d, rinv);
     if (prec == QS_PREC_C64) {
         if (truediv)
-            k_collapse<float2, true><<<grid, kT, 0, s>>>((float2*)state, npairs, target, outcome, d, rinv);
+            k_collapse<float2, true><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv);
         else
-            k_collapse<float2, false><<<grid, kT, 0, s>>>((float2*)state, npairs, target, outcome, d, rinv);
+            k_collapse<float2, false><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv);
     } else {
         if (truediv)
-            k_collapse<double2, true><<<grid, kT, 0, s>>>((double2*)state, npairs, target, outcome, d, rinv);
+            k_collapse<double2, true><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv);
         else
-            k_collapse<double2, false><<<grid, kT, 0, s>>>((double2*)state, npairs, target, outcome, d, rinv);
+            k_collapse<double2, false><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv);
     }
     return counted(cudaGetLastError());
+}
+
+cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int outcome, double d, double rinv,
+                                  int next_target, double* partials, int max_partials, double* out, cudaStream_t s,
+                                  int sms, uint64_t zmask, uint64_t zval) {
+    const IndexMap map = subspace_map(target, zmask, zval);
+    const uint64_t npairs = subspace_pairs(n, target, zmask);
+    const uint64_t tb = 1ull << target, ntb = 1ull << next_target;
+    int grid = grid_cap(npairs, sms, 2);
+    if (grid > max_partials) grid = max_partials;
+    const bool truediv = use_truediv(d, rinv);
+    if (prec == QS_PREC_C64) {
+        if (truediv)
+            k_collapse_probs<float2, true><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv, ntb,
+                                                                partials);
+        else
+            k_collapse_probs<float2, false><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv, ntb,
+                                                                 partials);
+    } else {
+        if (truediv)
+            k_collapse_probs<double2, true><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv,
+                                                                 ntb, partials);
+        else
+            k_collapse_probs<double2, false><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv,
+                                                                  ntb, partials);
+    }
+    k_prob_final<<<1, kT, 0, s>>>(partials, grid, out);
+    return counted(cudaGetLastError(), 2);
 }
 
 // ---------------------------------------------------------------- read-back

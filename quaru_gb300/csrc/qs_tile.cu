@@ -598,7 +598,9 @@ static bool df64_range_ok(const OpDesc& op) {
 int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>& ops,
               const std::vector<TileStage>& stages, cudaStream_t s, int sms, std::string* msg,
               const std::vector<float>* block_frags, int* derr_dev) {
-    int rep = (prec == QS_PREC_C64) ? 3 : (arith == QS_ARITH_EXACT ? 0 : (arith == QS_ARITH_FMA ? 1 : 2));
+    // tile arithmetic: exact order, FP64 FMA (also for QS_ARITH_FX64, whose one-gate sweeps are
+    // fixed-point), double-float, complex64
+    int rep = (prec == QS_PREC_C64) ? 3 : (arith == QS_ARITH_EXACT ? 0 : (arith == QS_ARITH_DF64 ? 2 : 1));
     if (rep == 2)
         for (const auto& op : ops)
             if (!df64_range_ok(op)) rep = 1;  // entries outside double-float range: FP64 FMA instead

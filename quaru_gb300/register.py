@@ -195,8 +195,32 @@ class Register:
         return measures
 
     def measure_circuit(self, circuit) -> list:
-        """Register::measure_circuit (src/register.rs:371-377)."""
-        return [(t, self.measure(t)) for t in circuit.get_measurement_targets()]
+        """Register::measure_circuit (src/register.rs:371-377): one qs_measure_sequence call."""
+        targets = list(circuit.get_measurement_targets())
+        return list(zip(targets, self.measure_sequence(targets)))
+
+    def measure_sequence(self, targets, draws=None) -> list:
+        """Measure targets in order (qs_measure_sequence) with the given draws (default: this
+        register's generator, one draw per target); returns the outcomes."""
+        targets = [int(t) for t in targets]
+        if draws is None:
+            draws = [self._rng() for _ in targets]
+        tg = np.array(targets, dtype=np.uintp)
+        dr = np.array(draws, dtype=np.float64)
+        if dr.size != tg.size:
+            raise ValueError("one draw per target")
+        out = np.zeros(tg.size, dtype=np.int32)
+        p0 = np.zeros(tg.size, dtype=np.float64)
+        p1 = np.zeros(tg.size, dtype=np.float64)
+        err = np.zeros(3, dtype=np.uintp)
+        try:
+            _check(_lib.load().qs_measure_sequence(self._h, _sp(tg), tg.size, _dp(dr),
+                                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(p0),
+                                                   _dp(p1), _sp(err)), err)
+        except OperationError as e:
+            raise RuntimeError("Could not measure bit") from e
+        self.last_sequence_probs = list(zip(p0.tolist(), p1.tolist()))
+        return [bool(x) for x in out]
 
     # ---- measurement (src/register.rs:291-342)
     def try_measure(self, target: int, draw: float | None = None) -> bool:
@@ -429,3 +453,16 @@ def _pauli_array(terms):
         arr[i].x_mask = int(x)
         arr[i].z_mask = int(z)
     return arr
+
+
+def circuit_autotune(n: int, precision: int = _lib.QS_PREC_C128, arith: int = _lib.QS_ARITH_FMA, fuse: int = 3,
+                     retune: bool = False) -> dict:
+    """qs_circuit_autotune: the fusion form qs_apply_circuit uses for this size, precision and arithmetic
+    (fuse 1: tile size, 2: block width, 3: any form), with each candidate's measured time when the
+    candidates were timed by this call."""
+    rep = _lib.QsAutotuneReport()
+    _check(_lib.load().qs_circuit_autotune(n, precision, arith, fuse, int(retune), ctypes.byref(rep)))
+    cands = [{"fuse": rep.cand_fuse[i], "max_width": rep.cand_width[i], "tile_qubits": rep.cand_tile[i],
+              "ms": rep.cand_ms[i]} for i in range(rep.count)]
+    return {"fuse": rep.fuse, "max_width": rep.max_width, "tile_qubits": rep.tile_qubits,
+            "from_cache": bool(rep.from_cache), "candidates": cands}

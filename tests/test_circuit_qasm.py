@@ -74,6 +74,30 @@ def test_reduction_passes_match_reference_behaviour():  # src/operation.rs:600-6
     assert len(c.reduce_circuit_cancel_gates().get_operations()) == 0
 
 
+def test_combining_overlapping_gates():  # src/operation.rs:114-178
+    from quaru_gb300 import operation as O
+    from quaru_gb300.circuit import QuantumCircuit
+
+    # a 1-qubit gate followed by an overlapping 2-qubit gate: one 4x4 operation on the larger
+    # gate's targets, equal to applying the two in circuit order
+    c = QuantumCircuit()
+    c.add_operation(O.hadamard(0))
+    c.add_operation(O.cnot(0, 1))
+    ops = c.reduce_gates_with_one_off_size(2).get_operations()
+    assert len(ops) == 1 and list(ops[0].targets) == [1, 0]
+    h = np.array(O.hadamard(0).matrix)
+    want = np.array(O.cnot(0, 1).matrix) @ np.kron(h, np.eye(2))
+    assert np.allclose(ops[0].matrix, want, atol=0)
+    # overlapping gates of equal arity cannot be combined: the reference's combine_ops multiplies a
+    # 4x4 by an 8x8 matrix and ndarray panics; here it raises
+    for second in (O.cnot(1, 2), O.swap(0, 1)):
+        c = QuantumCircuit()
+        c.add_operation(O.cnot(0, 1))
+        c.add_operation(second)
+        with pytest.raises(RuntimeError, match="equal arity"):
+            c.reduce_gates_with_one_off_size(2)
+
+
 @pytest.mark.gpu
 def test_bell_program_and_broadcast():
     from quaru_gb300.openqasm import run_openqasm_source

@@ -34,8 +34,21 @@ def test_gpu_matches_golden_bit_exact():
         bits.append(int(reg.measure(qb, draws[qb])))
         p0, p1 = reg.last_probs
         r0, r1 = (float.fromhex(x) for x in doc["measure_probs"][qb])
-        assert abs(p0 - r0) <= 1e-14 and abs(p1 - r1) <= 1e-14
+        assert p0 == r0 and p1 == r1  # sequential sums in the reference's order
     assert bits == doc["bitstring"]
+    assert sha(reg.state) == doc["sha256_after_measure"]  # the collapsed state, bit for bit
+
+
+@pytest.mark.gpu
+def test_gpu_measure_sequence_matches_golden_bit_exact():
+    import quaru_gb300 as q
+
+    doc, gates, draws = load_config1()
+    reg = q.Register.from_int(doc["n"], 0)
+    reg.apply_gates(gates)
+    bits = reg.measure_sequence(list(range(doc["n"])), draws)
+    assert [int(b) for b in bits] == doc["bitstring"]
+    assert sha(reg.state) == doc["sha256_after_measure"]
 
 
 @pytest.mark.gpu

@@ -105,3 +105,43 @@ def test_batch_rejects_unsupported_gates():
         Batch([(3, [ParamGate.fixed(O.swap(0, 1))], 0, [(1.0, 0, 1)])])
     with pytest.raises(q.EngineError):
         Batch([(3, [ParamGate.ry(0, 2)], 1, [(1.0, 0, 1)])])
+
+
+def _energy(n, gates, params, terms, precision=0):
+    import quaru_gb300 as q
+
+    reg = q.Register.from_int(n, 0, precision=precision)
+    reg.set_arith(q.QS_ARITH_FMA)
+    reg.apply_gates([g.operation(params) for g in gates])
+    return reg.expval_pauli(terms)
+
+
+def test_batch_at_the_benchmark_size():
+    """The benchmark's batch itself: 256 circuits of 10..22 qubits with 4..12 layers (config5's defaults).
+    FP64 (autotuned chunking, as the benchmark runs it), complex128 double-float and complex64 batches
+    against the loop of FP64 single-circuit gradients; central finite differences (h = 1e-6) on
+    parameters of the three largest circuits within 1e-6."""
+    from quaru_gb300.batch import Batch
+    from quaru_gb300.workloads import config5
+
+    circuits, params = config5()
+    params = np.array(params)
+    re, rg = per_circuit(circuits, params, 0)
+    for precision, arith, tol, cl, ct in [(0, 1, 1e-10, 0, 0), (0, 2, 1e-10, 12, 2), (1, 1, 2e-4, 12, 2)]:
+        b = Batch(circuits, precision=precision, arith=arith, chunk_log2=cl, ctas_per_sm=ct)
+        e, g = b.run(params)
+        assert np.max(np.abs(e - re)) < tol, (precision, arith)
+        assert np.max(np.abs(g - rg)) < tol, (precision, arith)
+        del b
+    offs = np.cumsum([0] + [c[2] for c in circuits])
+    largest = sorted(range(len(circuits)), key=lambda i: -circuits[i][0])[:3]
+    h = 1e-6
+    for i in largest:
+        n, gates, npar, terms = circuits[i]
+        p = params[offs[i]:offs[i] + npar].copy()
+        for j in (0, npar // 2, npar - 1):
+            pp, pm = p.copy(), p.copy()
+            pp[j] += h
+            pm[j] -= h
+            fd = (_energy(n, gates, pp, terms) - _energy(n, gates, pm, terms)) / (2 * h)
+            assert abs(fd - rg[offs[i] + j]) < 1e-6, (i, j, fd, rg[offs[i] + j])

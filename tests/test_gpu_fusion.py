@@ -202,3 +202,40 @@ def test_dense_block_fusion_c128_double_float(n):
         g.set_arith(2)
         g.apply_gates(ops, fuse=2, max_width=w)
         assert floored_rel_err(g.state, o.state) <= 1e-12, w
+
+
+def _floored_err_chunked(got: np.ndarray, ref: np.ndarray, chunk: int = 1 << 24) -> float:
+    """floored_rel_err over large states, a chunk at a time (no state-sized temporaries)."""
+    n = int(np.log2(ref.size))
+    floor = 2.0 ** (-n / 2.0)
+    worst = 0.0
+    for i in range(0, ref.size, chunk):
+        r = ref[i:i + chunk]
+        worst = max(worst, float(np.max(np.abs(got[i:i + chunk] - r) / np.maximum(np.abs(r), floor))))
+    return worst
+
+
+def test_fusion_widths_at_28_qubits_match_unfused_fp64():
+    """The benchmark's 28-qubit fusion-width configuration (40 layers for stages and 2- and 3-qubit
+    blocks, 10 layers for 4- and 5-qubit blocks, double-float arithmetic as timed) against one FP64
+    FMA sweep per gate on the same gates, within the 1e-12 floored bound."""
+    import quaru_gb300 as q
+    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+
+    n = 28
+    refs = {}
+    for layers in (40, 10):
+        ops = flatten(layered_circuit(n, layers, seed_for(2)))
+        r = q.Register.from_int(n, 0)
+        r.set_arith(q.QS_ARITH_FMA)
+        r.apply_gates(ops, fuse=0)
+        refs[layers] = (ops, r.state)
+        del r
+    for fuse, width, layers in [(1, 5, 40), (2, 2, 40), (2, 3, 40), (2, 4, 10), (2, 5, 10)]:
+        ops, ref = refs[layers]
+        g = q.Register.from_int(n, 0)
+        g.set_arith(q.QS_ARITH_DF64)
+        g.apply_gates(ops, fuse=fuse, max_width=width)
+        err = _floored_err_chunked(g.state, ref)
+        del g
+        assert err <= 1e-12, (fuse, width, layers, err)

@@ -358,3 +358,28 @@ def test_df64_deep_layered_circuit(q, orc):
     st /= np.linalg.norm(st)
     o, g = run_pair(q, orc, 10, flatten(layered_circuit(10, 5, 7)), arith=2, state=st)
     assert floored_rel_err(g, o) <= 1e-12
+
+
+@pytest.fixture(scope="module")
+def layered18(orc):
+    """The benchmarks' layered family (Haar 1q on every qubit + CNOTs on a random matching) at its
+    full 40-layer depth on 18 qubits (1080 gates, the 28-qubit configuration's seed), on the oracle."""
+    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+
+    n = 18
+    ops = flatten(layered_circuit(n, 40, seed_for(2)))
+    o = orc.OracleRegister.from_int(n, 0)
+    for op in ops:
+        o.try_apply_fast(op.matrix, op.targets)
+    return n, ops, o.state
+
+
+@pytest.mark.parametrize("arith,fuse", [(1, 0), (2, 0), (3, 0), (1, 1), (2, 1), (3, 1), (1, 2), (2, 2), (3, 2)])
+def test_layered_family_full_depth_every_form(q, layered18, arith, fuse):
+    """FP64 FMA, double-float and fixed-point arithmetic; one sweep per gate, cache-blocked stages and
+    dense blocks: all within the 1e-12 floored bound of the oracle after 1080 gates."""
+    n, ops, ref = layered18
+    g = q.Register.from_int(n, 0)
+    g.set_arith(arith)
+    g.apply_gates(ops, fuse=fuse)
+    assert floored_rel_err(g.state, ref) <= 1e-12

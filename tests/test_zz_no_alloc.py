@@ -6,9 +6,12 @@ path where allocation and its implicit synchronisation are not allowed). They
 pass a state vector they allocated themselves and a device output; the
 library's partial sums live in a static device array. Here the test itself
 allocates the caller-side buffers with torch (the entry point allocates
-nothing) and checks that two calls in a row give the sums the register path
-(qs_measure_probabilities) gives, within the 1e-14 the measurement tests use.
-This file is named so that pytest collects it last.
+nothing) and checks that two calls in a row give exactly the sums the register
+path (qs_measure_probabilities) gives: both use the same grid and the same
+reduction order and read complex64 amplitudes exactly (subnormal floats
+included), so the doubles must be identical. n = 24 needs 4096 partial blocks,
+the most the static array holds. This file is named so that pytest collects it
+last.
 """
 from __future__ import annotations
 
@@ -19,12 +22,13 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-14
-
 
 def _state(rng, n):
     v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
-    return v / np.linalg.norm(v)
+    v /= np.linalg.norm(v)
+    # a few amplitudes far below the float normal range (2^-126): subnormal in complex64
+    v[1 % v.size] = 3e-40 + 2e-41j
+    return v
 
 
 def _register_probs(lib, reg, target):
@@ -43,7 +47,7 @@ def test_noalloc_matches_register_path_on_consecutive_calls(precision):
     lib = _lib.load()
     rng = np.random.default_rng(4242 + precision)
     np_dtype = np.complex128 if precision == 0 else np.complex64
-    for n in (1, 6, 13, 19):
+    for n in (1, 6, 13, 19, 24):
         st = _state(rng, n).astype(np_dtype)
         reg = q.Register.from_int(n, 0, precision=precision)
         reg.state = st.astype(np.complex128)
@@ -62,7 +66,7 @@ def test_noalloc_matches_register_path_on_consecutive_calls(precision):
                 assert rc == 0, _lib.last_error()
                 stream.synchronize()
                 got = out.cpu().numpy()
-                assert abs(got[0] - want[0]) <= TOL and abs(got[1] - want[1]) <= TOL
+                assert got[0] == want[0] and got[1] == want[1], (n, target, got, want)
 
 
 def test_noalloc_rejects_invalid_requests():
@@ -84,3 +88,9 @@ def test_noalloc_rejects_invalid_requests():
     assert lib.qs_measure_probabilities_noalloc(b, 41, 0, 0, o, None, errp) == 5
     assert lib.qs_measure_probabilities_noalloc(b, 4, 3, 0, o, None, errp) == 5
     assert "n must be" in _lib.last_error() or "precision" in _lib.last_error()
+    # misaligned state (8 bytes into a complex128 buffer) and misaligned out are refused on the host
+    b8 = ctypes.c_void_p(buf.data_ptr() + 8)
+    assert lib.qs_measure_probabilities_noalloc(b8, 3, 0, 0, o, None, errp) == 5
+    assert "aligned" in _lib.last_error()
+    o4 = ctypes.c_void_p(out.data_ptr() + 4)
+    assert lib.qs_measure_probabilities_noalloc(b, 3, 0, 0, o4, None, errp) == 5
