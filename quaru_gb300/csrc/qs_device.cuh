@@ -305,7 +305,7 @@ __device__ __forceinline__ long long fx_row_sum(const int32_t* vh, const int32_t
 
 // R * 2^k rounded to nearest double, any R (|R| < 2^63) and k: the conversion rounds R once, scalbn
 // scales exactly unless the result leaves the normal range.
-__device__ __noinline__ double fx_to_double_any(long long R, int k) {
+static __device__ __noinline__ double fx_to_double_any(long long R, int k) {
     return R == 0 ? 0.0 : scalbn(__ll2double_rn(R), k);
 }
 
