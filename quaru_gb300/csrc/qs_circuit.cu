@@ -108,7 +108,7 @@ static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* ga
         return QS_OK;
     }
     const int T = std::min(12, n), L = std::min(5, T);
-    std::vector<TileStage> stages = plan_tiles(ops, n, T, L, false);
+    std::vector<TileStage> stages = plan_tiles(ops, n, T, L, false, kMaxTcBlocks);
     return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg, &frags);
 }
 

@@ -177,6 +177,17 @@ __global__ void __launch_bounds__(kThreads, 6) k_dense1_fx(double2* __restrict__
         const double2 x0 = st[i0], x1 = st[i0 | a.tbit];
         double2 y0, y1;
         const uint32_t E = max(max(fx_efield(x0.x), fx_efield(x0.y)), max(fx_efield(x1.x), fx_efield(x1.y)));
+        if (E == 0u) {  // zeros and subnormals only; all four zero: every output is +0, as R = 0 gives
+            const uint32_t his = uint32_t(__double2hiint(x0.x) | __double2hiint(x0.y) | __double2hiint(x1.x) |
+                                          __double2hiint(x1.y)) & 0x7fffffffu;
+            const uint32_t los = uint32_t(__double2loint(x0.x) | __double2loint(x0.y) | __double2loint(x1.x) |
+                                          __double2loint(x1.y));
+            if ((his | los) == 0u) {
+                st[i0] = make_double2(0.0, 0.0);
+                st[i0 | a.tbit] = make_double2(0.0, 0.0);
+                continue;
+            }
+        }
         if (E >= kFxMinE && E < 0x7ffu && int(E) + a.kmin >= kFxFastKMin && int(E) + a.kmax <= kFxFastKMax) {
             int32_t vh[4], vl[4];
             fx_encode(x0.x, E, vh[0], vl[0]);

@@ -190,18 +190,17 @@ void block_fragments(const std::vector<double>& u, float* out) {
         if ((n < 32) == (k < 32)) return re;
         return (n < 32) ? -im : im;
     };
-    for (int nt = 0; nt < 8; nt++)
-        for (int ks = 0; ks < 8; ks++)
-            for (int lane = 0; lane < 32; lane++) {
-                const int g = lane >> 2, t = lane & 3;
-                const double v0 = M(8 * nt + g, 8 * ks + t), v1 = M(8 * nt + g, 8 * ks + t + 4);
-                const float h0 = tf32_rna(float(v0)), h1 = tf32_rna(float(v1));
-                float* o = out + 4 * ((nt * 8 + ks) * 32 + lane);
-                o[0] = h0;
-                o[1] = h1;
-                o[2] = tf32_rna(float(v0 - double(h0)));
-                o[3] = tf32_rna(float(v1 - double(h1)));
-            }
+    // B[n][k] = M[n][k] (output n, input k), K-major in core matrices of 8 rows x 4 elements, 16 of
+    // them along K per 8-row group: the shared-memory image the tensor-core descriptors read. The
+    // high TF32 parts first, then the low parts.
+    for (int n = 0; n < 64; n++)
+        for (int k = 0; k < 64; k++) {
+            const double v = M(n, k);
+            const float h = tf32_rna(float(v));
+            const int off = ((n >> 3) * 16 + (k >> 2)) * 32 + (n & 7) * 4 + (k & 3);
+            out[off] = h;
+            out[4096 + off] = tf32_rna(float(v - double(h)));
+        }
 }
 
 // Whether a stage op can be a register-pass member (k <= 1 dense or monomial).

@@ -1,0 +1,90 @@
+// qs_tc05.cuh — fifth-generation tensor cores (tcgen05) for sm_103a: tensor-memory allocation,
+// shared-memory matrix descriptors, single-thread MMA issue with mbarrier completion, and
+// tensor-memory loads.
+//
+// Operands live in shared memory in the canonical K-major layout without swizzling: the matrix is
+// cut into core matrices of 8 rows x 16 bytes (8 x 4 for 32-bit elements), each stored as 128
+// contiguous bytes (row r at byte 16 r). Core matrices adjacent along K are `lbo` bytes apart,
+// core matrices adjacent along M (or N) are `sbo` bytes apart. The accumulator D (M = 128 rows,
+// FP32) occupies tensor-memory lanes 0..127 (row i on lane i) and one column per output column.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qs_tma.cuh"
+
+namespace qs {
+
+// Shared-memory matrix descriptor (sm_100 family): start address, leading-dimension byte offset
+// (between core matrices along K) and stride-dimension byte offset (between 8-row groups along M
+// or N), all in 16-byte units; descriptor version 1 in bits 46-47; no swizzling (layout type 0).
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr_bytes, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = uint64_t((saddr_bytes & 0x3ffffu) >> 4);
+    d |= uint64_t((lbo >> 4) & 0x3fffu) << 16;
+    d |= uint64_t((sbo >> 4) & 0x3fffu) << 32;
+    d |= uint64_t(1) << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::tf32 with FP32 accumulation, both operands K-major, M x N.
+__host__ __device__ constexpr uint32_t tc_idesc_tf32(uint32_t M, uint32_t N) {
+    return (1u << 4)                // D format: F32
+           | (2u << 7)              // A format: TF32
+           | (2u << 10)             // B format: TF32
+           | ((N >> 3) << 17)       // N / 8
+           | ((M >> 4) << 24);      // M / 16
+}
+
+// Allocate `ncols` (power of two, >= 32) tensor-memory columns; the whole warp executes this and
+// the base address lands in *slot (shared memory).
+__device__ __forceinline__ void tc_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(slot)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D (+)= A * B for one K step (single thread).
+__device__ __forceinline__ void tc_mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// Arrive on `bar` once every MMA this thread issued so far has completed.
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+                 : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's lane: a warp reads lanes 32 (warp % 4) .. + 31.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Byte offset of element (row, k) of a K-major operand with 32-bit elements in the core-matrix
+// layout: core matrices of 8 rows x 4 elements, `kcm` of them along K per 8-row group.
+__host__ __device__ __forceinline__ uint32_t tc_kmajor_off(uint32_t row, uint32_t k, uint32_t kcm) {
+    return ((row >> 3) * kcm + (k >> 2)) * 128u + (row & 7u) * 16u + (k & 3u) * 4u;
+}
+
+}  // namespace qs

@@ -23,6 +23,7 @@
 #include "qs_kernels.h"
 #include "qs_tile.h"
 #include "qs_pass.cuh"
+#include "qs_tc05.cuh"
 #include "qs_tma.cuh"
 
 namespace qs {
@@ -257,15 +258,6 @@ __device__ __forceinline__ uint32_t f2tf32(float x) {
     return r;
 }
 
-__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
 __device__ __forceinline__ uint32_t deposit5(uint32_t r, const uint8_t* pos) {
     uint32_t o = 0;
 #pragma unroll
@@ -273,63 +265,68 @@ __device__ __forceinline__ uint32_t deposit5(uint32_t r, const uint8_t* pos) {
     return o;
 }
 
-// Y = U X for the 32-row block view of the tile: X^T (columns x 64 real) times
-// B = M^T, M = [[Ur, -Ui], [Ui, Ur]]; D = A_lo B_hi + A_hi B_lo + A_hi B_hi in FP32.
-// Warp w owns m-tiles w, w + 8, ... (16 columns each) and updates them in place.
-__device__ __forceinline__ void block_apply(float* sf, uint32_t tsize, const TileOp& op,
-                                            const float4* __restrict__ bfrag) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const uint32_t nmt = (tsize >> 5) >> 4;
+__device__ __forceinline__ int warp_id() { return int(threadIdx.x >> 5); }
+
+// Operand images of the tensor-core blocks (qs_tc05.cuh layout): A = the tile's block view, 128
+// columns x 64 reals (32 real parts, 32 imaginary parts of the block rows), B = the block matrix.
+constexpr uint32_t kTcABytes = 128u * 64u * 4u;  // one A image (high or low TF32 parts)
+constexpr uint32_t kTcBBytes = 64u * 64u * 4u;   // one B image
+constexpr uint32_t kTcLbo = 128u, kTcSbo = 2048u, kTcCols = 64u;
+
+// Y = U X for the 32-row block view of a 12-qubit complex64 tile on the tensor cores (3xTF32):
+// D = A_lo B_hi + A_hi B_lo + A_hi B_hi accumulated in FP32 in tensor memory, where A (128 x 64)
+// holds the tile's columns (the 7 bits outside the block) by their 64 real block components, split
+// once into TF32 high and low parts, and B (64 x 64) is the block's [[Ur, -Ui], [Ui, Ur]]. One
+// thread issues the 24 MMAs and commits them to `bar`; all warps then read D back into the tile.
+// False when the bounded wait for the MMAs gave up (the tile is left unchanged).
+__device__ __forceinline__ bool block_apply_tc(float* sf, const TileOp& op, float* sa, const float* sb, uint64_t* bar,
+                                               uint32_t* parity, uint32_t tmem) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint8_t pos[5];
 #pragma unroll
     for (int b = 0; b < 5; b++) pos[b] = op.pos[b];
-    uint32_t rd[8], wr[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) rd[j] = deposit5(uint32_t(4 * j + t), pos);
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        wr[2 * q] = deposit5(uint32_t(8 * q + 2 * t), pos);
-        wr[2 * q + 1] = deposit5(uint32_t(8 * q + 2 * t + 1), pos);
+    // A: one core matrix (8 columns x 4 components) per warp store, 128 contiguous bytes
+    for (uint32_t cm = warp; cm < 256u; cm += kTileThreads / 32) {
+        const uint32_t m = 8u * (cm >> 4) + uint32_t(lane >> 2), k = 4u * (cm & 15u) + uint32_t(lane & 3);
+        const uint32_t idx = expand_local(m, pos, 5) | deposit5(k & 31u, pos);
+        const float a = sf[2 * idx + (k >> 5)];
+        const float h = __uint_as_float(f2tf32(a));
+        sa[cm * 32u + uint32_t(lane)] = h;
+        sa[kTcABytes / 4 + cm * 32u + uint32_t(lane)] = __uint_as_float(f2tf32(a - h));
     }
-    const float4* bf = bfrag + op.bidx + lane;
-    for (uint32_t mt = warp; mt < nmt; mt += kTileThreads / 32) {
-        const uint32_t c0 = expand_local(16 * mt + g, pos, 5);
-        const uint32_t c1 = expand_local(16 * mt + g + 8, pos, 5);
-        float acc[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    fence_async_shared();  // the tensor cores read shared memory through the async proxy
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x == 0) {
+        constexpr uint32_t idesc = tc_idesc_tf32(128, 64);
+        const uint32_t ah = saddr(sa), al = ah + kTcABytes, bh = saddr(sb), bl = bh + kTcBBytes;
 #pragma unroll 1
-        for (int comp = 0; comp < 2; comp++) {  // k-steps 0..3 read real parts, 4..7 imaginary parts
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int ks = 4 * comp + q;
-                const float a0 = sf[2 * (c0 | rd[2 * q]) + comp], a1 = sf[2 * (c1 | rd[2 * q]) + comp];
-                const float a2 = sf[2 * (c0 | rd[2 * q + 1]) + comp], a3 = sf[2 * (c1 | rd[2 * q + 1]) + comp];
-                const uint32_t h0 = f2tf32(a0), h1 = f2tf32(a1), h2 = f2tf32(a2), h3 = f2tf32(a3);
-                const uint32_t l0 = f2tf32(a0 - __uint_as_float(h0)), l1 = f2tf32(a1 - __uint_as_float(h1));
-                const uint32_t l2 = f2tf32(a2 - __uint_as_float(h2)), l3 = f2tf32(a3 - __uint_as_float(h3));
-#pragma unroll
-                for (int nt = 0; nt < 8; nt++) {
-                    const float4 b = __ldg(bf + (nt * 8 + ks) * 32);
-                    const uint32_t bh0 = __float_as_uint(b.x), bh1 = __float_as_uint(b.y);
-                    const uint32_t bl0 = __float_as_uint(b.z), bl1 = __float_as_uint(b.w);
-                    mma_tf32(acc[nt], l0, l1, l2, l3, bh0, bh1);
-                    mma_tf32(acc[nt], h0, h1, h2, h3, bl0, bl1);
-                    mma_tf32(acc[nt], h0, h1, h2, h3, bh0, bh1);
-                }
-            }
+        for (uint32_t ks = 0; ks < 8; ks++) {  // K = 8 per MMA: two core matrices along K
+            const uint32_t o = ks * 2u * kTcLbo;
+            tc_mma_tf32(tmem, tc_smem_desc(al + o, kTcLbo, kTcSbo), tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, ks);
+            tc_mma_tf32(tmem, tc_smem_desc(ah + o, kTcLbo, kTcSbo), tc_smem_desc(bl + o, kTcLbo, kTcSbo), idesc, 1);
+            tc_mma_tf32(tmem, tc_smem_desc(ah + o, kTcLbo, kTcSbo), tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, 1);
         }
-        __syncwarp();
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-            const int comp = nt >> 2, q = nt & 3;
-            sf[2 * (c0 | wr[2 * q]) + comp] = acc[nt][0];
-            sf[2 * (c0 | wr[2 * q + 1]) + comp] = acc[nt][1];
-            sf[2 * (c1 | wr[2 * q]) + comp] = acc[nt][2];
-            sf[2 * (c1 | wr[2 * q + 1]) + comp] = acc[nt][3];
-        }
-        __syncwarp();
+        tc_commit(bar);
     }
+    const bool ok = mbar_wait_bounded(bar, *parity);
+    *parity ^= 1u;
+    tc_fence_after();
+    if (ok) {
+        // warp w reads tensor-memory lanes 32 (w % 4) .. (columns of the tile) and D columns
+        // 32 (w / 4) .. (real parts for warps 0-3, imaginary parts for warps 4-7)
+        float v[32];
+        const uint32_t row0 = 32u * uint32_t(warp & 3), comp = uint32_t(warp >> 2);
+        tc_ld32(tmem + (row0 << 16) + 32u * comp, v);
+        const uint32_t cb = expand_local(row0 + uint32_t(lane), pos, 5);
+#pragma unroll
+        for (int j = 0; j < 32; j++) sf[2 * (cb | deposit5(uint32_t(j), pos)) + comp] = v[j];
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    return ok;
 }
 
 // Element type of the state in global memory (the tile buffer holds it while a copy is in flight).
@@ -380,12 +377,45 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
     // rows: each bulk copy costs the copy engine ~90 cycles, so all threads move the tile in 16-byte
     // pieces (cp.async in, shared loads + global stores out), two tiles ahead in a ring of three.
     const bool bulk = nrows <= 8;
+    // Tensor-core blocks: after the row offsets (1 KiB aligned) the stage's B images (32 KiB per
+    // block op), the A images (64 KiB), an mbarrier for the B copies and one for the MMAs, and the
+    // tensor-memory address.
+    float* tcB = nullptr;
+    float* tcA = nullptr;
+    uint64_t* tcbar = nullptr;
+    uint32_t* tslot = nullptr;
+    if constexpr (BLK) {
+        unsigned char* p = reinterpret_cast<unsigned char*>(rowoff + nrows);
+        p += (1024u - (saddr(p) & 1023u)) & 1023u;
+        tcB = reinterpret_cast<float*>(p);
+        tcA = reinterpret_cast<float*>(p + size_t(nops) * 2 * kTcBBytes);
+        tcbar = reinterpret_cast<uint64_t*>(p + size_t(nops) * 2 * kTcBBytes + 2 * kTcABytes);
+        tslot = reinterpret_cast<uint32_t*>(tcbar + 2);
+        if (warp_id() == 0) tc_alloc(tslot, kTcCols);
+    }
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) mbar_init(&mbar[b], bulk ? 1 : kTileThreads);
+        if constexpr (BLK) {
+            mbar_init(&tcbar[0], 1);
+            mbar_init(&tcbar[1], 1);
+        }
         fence_mbar_init();
         s_abort = 0;
     }
+    if constexpr (BLK) tc_fence_before();
     __syncthreads();
+    uint32_t tmem = 0, mma_parity = 0;
+    if constexpr (BLK) {
+        tc_fence_after();
+        tmem = *tslot;
+        if (threadIdx.x == 0) {  // the stage's block operands, loaded once per CTA
+            mbar_expect_tx(&tcbar[0], uint32_t(nops) * 2u * kTcBBytes);
+            for (int o = 0; o < nops; o++)
+                bulk_load(tcB + size_t(o) * 2 * kTcBBytes / 4, bfrag + sops[o].bidx, 2 * kTcBBytes, &tcbar[0]);
+        }
+        if (!mbar_wait_bounded(&tcbar[0], 0)) atomicOr(&s_abort, 1);
+        __syncthreads();
+    }
     const uint64_t first = blockIdx.x;
     const uint64_t nmy = (ntiles > first) ? (ntiles - 1 - first) / gridDim.x + 1 : 0;
     const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.RL;
@@ -465,7 +495,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
             const int kind = op.kind;
             if (BLK) {
                 if constexpr (REP == 3 && BLK)
-                    if (kind == OP_BLOCK) block_apply(reinterpret_cast<float*>(s), tsize, op, bfrag);
+                    if (kind == OP_BLOCK &&
+                        !block_apply_tc(reinterpret_cast<float*>(s), op, tcA, tcB + size_t(o) * 2 * kTcBBytes / 4,
+                                        &tcbar[1], &mma_parity, tmem))
+                        s_abort = 1;
             } else if (REP == 3 && kind == OP_PASS) {
                 if constexpr (REP == 3 && !BLK) pass_run_c64(reinterpret_cast<float2*>(s), tsize, &base, &sops[o]);
                 o += op.k;
@@ -536,6 +569,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
         cp_async_wait_all();  // copies of tiles the loop did not reach
         if (s_abort && threadIdx.x == 0) atomicExch(err, 1);
     }
+    if constexpr (BLK) {  // every warp is done with tensor memory: release it
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (warp_id() == 0) tc_dealloc(tmem, kTcCols);
+    }
 }
 
 static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
@@ -571,7 +610,11 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     const size_t fixed = 4 * sizeof(uint64_t) + sizeof(TileOp) * size_t(op_end - op_begin) +
                          (sizeof(uint64_t) << sa.RH);
     sa.nbuf = (3 * tile_bytes + fixed <= 110 * 1024) ? 3 : 2;  // three buffers where two blocks still fit an SM
-    const size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
+    size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
+    if (BLK) {  // two tile buffers, then the resident block operands (one CTA per SM)
+        sa.nbuf = 2;
+        smem = 2 * tile_bytes + fixed + 1024 + size_t(op_end - op_begin) * 2 * kTcBBytes + 2 * kTcABytes + 32;
+    }
     const uint64_t ntiles = 1ull << (n - st.T);
     // One wave exactly: every CTA walks the same number of tiles, so a grid larger than what is
     // resident would leave a second, partly empty wave.

@@ -79,10 +79,14 @@ struct alignas(16) TileOp {
     uint32_t bidx;       // OP_BLOCK: offset of the block's B fragments (float4 units)
 };
 
-// Tensor-core fragments of one fused 5-qubit block: [n-tile 8][k-step 8][lane 32] float4
-// (b0_hi, b1_hi, b0_lo, b1_lo) of B = M^T, M = [[Ur, -Ui], [Ui, Ur]] (64 x 64 real).
+// Tensor-core operand of one fused 5-qubit block: B = M, M = [[Ur, -Ui], [Ui, Ur]] (64 x 64 real,
+// output n x input k), as two K-major core-matrix images (TF32 high parts, then low parts) of
+// 4096 floats each; 32 KiB in all (kBlockFragFloat4 float4s).
 constexpr uint32_t kBlockFragFloat4 = 8 * 8 * 32;
 void block_fragments(const std::vector<double>& u32x32, float* out /* 4 * kBlockFragFloat4 floats */);
+
+// Fused blocks per tensor-core stage: the stage's B images stay resident in shared memory.
+constexpr int kMaxTcBlocks = 2;
 
 struct TileStage {
     bool tiled = false;
