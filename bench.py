@@ -416,8 +416,32 @@ def run_ours(args) -> None:
 
     peak, peak_kind = read_peaks()
     forms = None
+    fx_layer = None
     if prec == q.QS_PREC_C128 and not args.no_forms:
         forms = dense1_forms(q, torch, reg, layers, n, peak)
+        # the same timed layers in the FP64-accurate fixed-point form (CNOTs stay index moves)
+        reg.set_arith(q.QS_ARITH_FX64)
+        for i in range(args.warmup):
+            for g in layer(i):
+                reg.try_apply_fast(g)
+        barrier()
+        x0 = torch.cuda.Event(enable_timing=True)
+        x1 = torch.cuda.Event(enable_timing=True)
+        x0.record(stream)
+        for i in range(args.warmup, args.warmup + args.steps):
+            for g in layer(i):
+                reg.try_apply_fast(g)
+        x1.record(stream)
+        barrier()
+        xs = x0.elapsed_time(x1) / 1e3
+        fx_ms = forms["fx64"]["ms"]
+        fx_layer = {"value": step_bytes / xs / 1e9, "unit": UNIT, "ms_per_step": 1e3 * xs / args.steps,
+                    "gates_per_s": len(layer(0)) * args.steps / xs, "arith": ARITH_DTYPE["fx64"],
+                    "roofline": {"kernel": "k_dense1_fx (dense 1-qubit gate sweep, c128, fixed-point arithmetic)",
+                                 "bound": "hbm", "achieved": forms["fx64"]["gbs"], "peak": peak, "unit": "GB/s",
+                                 "frac": forms["fx64"]["gbs"] / peak, "traffic": read_traffic("c128", "fx64"),
+                                 "peak_source": peak_kind, "bytes_per_launch": 2.0 * (1 << n) * 16,
+                                 "ms_per_launch": fx_ms}}
         reg.set_arith(arith)
     del reg
     torch.cuda.synchronize()
@@ -480,6 +504,7 @@ def run_ours(args) -> None:
                      "fp64_pipe_peak_tflops_measured": FP64_PEAK_TFLOPS_MEASURED},
         "kernel_ms": {"dense1_avg": avg_haar_s * 1e3, "samples": len(haar_ms)},
         "dense1_forms": forms,
+        "fp64_accurate_fx64": fx_layer,
         "autotune": tuned,
         "measure": meas,
         "clocks": clk,
@@ -780,6 +805,43 @@ def run_kernels(args) -> None:
     print(json.dumps({"kernels": "done", "qubits": n, "launches": int(q._lib.load().qs_launch_count())}))
 
 
+def run_case(args) -> None:
+    """Small profiling workloads (for ncu captures of one kernel family, --qubits 26 by default):
+    dense-<arith>: four dense 1-qubit Haar sweeps on a dense complex128 register in that arithmetic;
+    blocks-c64: two layers of the family as 5-qubit 3xTF32 blocks on a complex64 register;
+    stages-c64: the same layers as register passes; measure-all: every qubit of a dense complex128
+    register measured in one sequence."""
+    import quaru_gb300 as q
+    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+
+    n = args.qubits
+    if args.case.startswith("dense-"):
+        arith = ARITH_CODES(q)[args.case.split("-", 1)[1]]
+        layer = layered_circuit(n, 1, seed_for(3))[0]
+        r = q.Register.from_int(n, 0)
+        r.set_arith(q.QS_ARITH_DF64)
+        r.apply_gates(layer)  # a dense state
+        r.set_arith(arith)
+        for g in [g for g in layer if is_haar(g)][:4]:
+            r.try_apply_fast(g)
+    elif args.case in ("blocks-c64", "stages-c64"):
+        r = q.Register.from_int(n, 0, precision=q.QS_PREC_C64)
+        ops = flatten(layered_circuit(n, 2, seed_for(3)))
+        if args.case == "blocks-c64":
+            r.apply_gates(ops, fuse=2, max_width=5)
+        else:
+            r.apply_gates(ops, fuse=1, tile_qubits=12)
+    elif args.case == "measure-all":
+        r = q.Register.from_int(n, 0)
+        r.set_arith(q.QS_ARITH_FMA)
+        r.apply_gates(flatten(layered_circuit(n, 1, seed_for(3))))
+        r.measure_sequence(list(range(n)), [0.5] * n)
+    else:
+        raise SystemExit(f"unknown case {args.case}")
+    r.synchronize()
+    print(json.dumps({"case": args.case, "qubits": n, "launches": int(q._lib.load().qs_launch_count())}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -805,6 +867,7 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-gradient section")
     ap.add_argument("--no-widths", action="store_true", help="skip the 28-qubit fusion-width section")
     ap.add_argument("--kernels", action="store_true", help="run the per-kernel profiling workload instead")
+    ap.add_argument("--case", help="run one small profiling workload instead (see run_case)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps are required")
@@ -816,6 +879,8 @@ def main() -> None:
         run_reference(args)
     elif args.kernels:
         run_kernels(args)
+    elif args.case:
+        run_case(args)
     else:
         run_ours(args)
 
