@@ -267,46 +267,63 @@ __device__ __forceinline__ uint32_t deposit5(uint32_t r, const uint8_t* pos) {
 
 __device__ __forceinline__ int warp_id() { return int(threadIdx.x >> 5); }
 
-// Operand images of the tensor-core blocks (qs_tc05.cuh layout): A = the tile's block view, 128
-// columns x 64 reals (32 real parts, 32 imaginary parts of the block rows), B = the block matrix.
-constexpr uint32_t kTcABytes = 128u * 64u * 4u;  // one A image (high or low TF32 parts)
+// Operand image of a tensor-core block in shared memory (qs_tc05.cuh layout): the block matrix B.
 constexpr uint32_t kTcBBytes = 64u * 64u * 4u;   // one B image
-constexpr uint32_t kTcLbo = 128u, kTcSbo = 2048u, kTcCols = 64u;
+constexpr uint32_t kTcLbo = 128u, kTcSbo = 2048u;
+// Tensor-memory columns of one group: D (64 FP32 columns), then the A high and low parts.
+constexpr uint32_t kTcAHi = 64u, kTcALo = 128u, kTcGroupCols = 256u;
 
-// Y = U X for the 32-row block view of a 12-qubit complex64 tile on the tensor cores (3xTF32):
-// D = A_lo B_hi + A_hi B_lo + A_hi B_hi accumulated in FP32 in tensor memory, where A (128 x 64)
-// holds the tile's columns (the 7 bits outside the block) by their 64 real block components, split
-// once into TF32 high and low parts, and B (64 x 64) is the block's [[Ur, -Ui], [Ui, Ur]]. One
-// thread issues the 24 MMAs and commits them to `bar`; all warps then read D back into the tile.
-// False when the bounded wait for the MMAs gave up (the tile is left unchanged).
-__device__ __forceinline__ bool block_apply_tc(float* sf, const TileOp& op, float* sa, const float* sb, uint64_t* bar,
-                                               uint32_t* parity, uint32_t tmem) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// Float offsets of a block op inside the tile: column m (the 7 tile bits outside the block, 0..127)
+// starts at cof[m], block row j (0..31) adds rof[j]; the real part sits at the offset, the
+// imaginary part one float further. Built once per CTA for each block op of the stage.
+constexpr int kTcIdxWords = 128 + 32;
+__device__ __forceinline__ void block_index_table(const TileOp& op, uint32_t* tab, int nthreads) {
     uint8_t pos[5];
 #pragma unroll
     for (int b = 0; b < 5; b++) pos[b] = op.pos[b];
-    // A: one core matrix (8 columns x 4 components) per warp store, 128 contiguous bytes
-    for (uint32_t cm = warp; cm < 256u; cm += kTileThreads / 32) {
-        const uint32_t m = 8u * (cm >> 4) + uint32_t(lane >> 2), k = 4u * (cm & 15u) + uint32_t(lane & 3);
-        const uint32_t idx = expand_local(m, pos, 5) | deposit5(k & 31u, pos);
-        const float a = sf[2 * idx + (k >> 5)];
-        const float h = __uint_as_float(f2tf32(a));
-        sa[cm * 32u + uint32_t(lane)] = h;
-        sa[kTcABytes / 4 + cm * 32u + uint32_t(lane)] = __uint_as_float(f2tf32(a - h));
+    for (int i = threadIdx.x; i < kTcIdxWords; i += nthreads)
+        tab[i] = i < 128 ? 2u * expand_local(uint32_t(i), pos, 5) : 2u * deposit5(uint32_t(i - 128), pos);
+}
+
+// Y = U X for the 32-row block view of a 12-qubit complex64 tile on the tensor cores (3xTF32), by
+// one group of kTcGroupThreads threads: D = A_lo B_hi + A_hi B_lo + A_hi B_hi accumulated in FP32
+// in tensor memory. A (128 x 64) holds the tile's 128 columns (the 7 tile bits outside the block)
+// by their 64 real block components (32 real parts, 32 imaginary parts), split once into TF32 high
+// and low parts and stored straight into the group's tensor-memory columns; B (64 x 64, the
+// block's [[Ur, -Ui], [Ui, Ur]]) is resident in shared memory. Warp w of the group owns tile
+// column (lane) 32 (w % 4) + lane and the real (w < 4) or imaginary (w >= 4) components. One
+// thread issues the 24 MMAs and commits them to `bar`; the group then reads D back into the tile.
+// False when the bounded wait for the MMAs gave up (the tile is left unchanged).
+constexpr int kTcGroupThreads = 256;
+__device__ __forceinline__ bool block_apply_tc(float* sf, const uint32_t* tab, const float* sb, uint64_t* bar,
+                                               uint32_t* parity, uint32_t tcol, int gt, int barrier_id) {
+    const int gw = gt >> 5, lane = gt & 31;
+    const uint32_t quarter = uint32_t(gw & 3) << 21;  // lane base 32 (w % 4), in bits 16.. of the address
+    const uint32_t comp = uint32_t(gw >> 2);
+    const uint32_t col = tab[32 * (gw & 3) + lane] + comp;
+    {
+        float hi[32], lo[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const float a = sf[col + tab[128 + j]];
+            hi[j] = __uint_as_float(f2tf32(a));
+            lo[j] = __uint_as_float(f2tf32(a - hi[j]));
+        }
+        tc_st32(tcol + quarter + kTcAHi + 32u * comp, hi);
+        tc_st32(tcol + quarter + kTcALo + 32u * comp, lo);
     }
-    fence_async_shared();  // the tensor cores read shared memory through the async proxy
     tc_fence_before();
-    __syncthreads();
+    named_sync(barrier_id, kTcGroupThreads);
     tc_fence_after();
-    if (threadIdx.x == 0) {
+    if (gt == 0) {
         constexpr uint32_t idesc = tc_idesc_tf32(128, 64);
-        const uint32_t ah = saddr(sa), al = ah + kTcABytes, bh = saddr(sb), bl = bh + kTcBBytes;
+        const uint32_t bh = saddr(sb), bl = bh + kTcBBytes;
 #pragma unroll 1
-        for (uint32_t ks = 0; ks < 8; ks++) {  // K = 8 per MMA: two core matrices along K
+        for (uint32_t ks = 0; ks < 8; ks++) {  // K = 8 per MMA
             const uint32_t o = ks * 2u * kTcLbo;
-            tc_mma_tf32(tmem, tc_smem_desc(al + o, kTcLbo, kTcSbo), tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, ks);
-            tc_mma_tf32(tmem, tc_smem_desc(ah + o, kTcLbo, kTcSbo), tc_smem_desc(bl + o, kTcLbo, kTcSbo), idesc, 1);
-            tc_mma_tf32(tmem, tc_smem_desc(ah + o, kTcLbo, kTcSbo), tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, 1);
+            tc_mma_tf32_ta(tcol, tcol + kTcALo + 8u * ks, tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, ks);
+            tc_mma_tf32_ta(tcol, tcol + kTcAHi + 8u * ks, tc_smem_desc(bl + o, kTcLbo, kTcSbo), idesc, 1);
+            tc_mma_tf32_ta(tcol, tcol + kTcAHi + 8u * ks, tc_smem_desc(bh + o, kTcLbo, kTcSbo), idesc, 1);
         }
         tc_commit(bar);
     }
@@ -314,17 +331,13 @@ __device__ __forceinline__ bool block_apply_tc(float* sf, const TileOp& op, floa
     *parity ^= 1u;
     tc_fence_after();
     if (ok) {
-        // warp w reads tensor-memory lanes 32 (w % 4) .. (columns of the tile) and D columns
-        // 32 (w / 4) .. (real parts for warps 0-3, imaginary parts for warps 4-7)
         float v[32];
-        const uint32_t row0 = 32u * uint32_t(warp & 3), comp = uint32_t(warp >> 2);
-        tc_ld32(tmem + (row0 << 16) + 32u * comp, v);
-        const uint32_t cb = expand_local(row0 + uint32_t(lane), pos, 5);
+        tc_ld32(tcol + quarter + 32u * comp, v);
 #pragma unroll
-        for (int j = 0; j < 32; j++) sf[2 * (cb | deposit5(uint32_t(j), pos)) + comp] = v[j];
+        for (int j = 0; j < 32; j++) sf[col + tab[128 + j]] = v[j];
     }
     tc_fence_before();
-    __syncthreads();
+    named_sync(barrier_id, kTcGroupThreads);
     tc_fence_after();
     return ok;
 }
@@ -343,11 +356,10 @@ struct GlobElem<3> {
 // warp 0 has already issued the bulk row copies of tile i + 1 into the other buffer (completion
 // on an mbarrier with expect-tx); finished tiles go back with bulk stores. Waits are bounded and
 // set *err instead of hanging.
-template <int REP, bool BLK>
+template <int REP>
 __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ state, uint64_t ntiles,
                                                        const __grid_constant__ StageArgs sa,
-                                                       const TileOp* __restrict__ ops,
-                                                       const float4* __restrict__ bfrag, int* __restrict__ err) {
+                                                       const TileOp* __restrict__ ops, int* __restrict__ err) {
     using E = typename TileElem<REP>::T;
     using GE = typename GlobElem<REP>::T;
     static_assert(sizeof(E) == sizeof(GE), "tile element and state element must have the same size");
@@ -377,45 +389,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
     // rows: each bulk copy costs the copy engine ~90 cycles, so all threads move the tile in 16-byte
     // pieces (cp.async in, shared loads + global stores out), two tiles ahead in a ring of three.
     const bool bulk = nrows <= 8;
-    // Tensor-core blocks: after the row offsets (1 KiB aligned) the stage's B images (32 KiB per
-    // block op), the A images (64 KiB), an mbarrier for the B copies and one for the MMAs, and the
-    // tensor-memory address.
-    float* tcB = nullptr;
-    float* tcA = nullptr;
-    uint64_t* tcbar = nullptr;
-    uint32_t* tslot = nullptr;
-    if constexpr (BLK) {
-        unsigned char* p = reinterpret_cast<unsigned char*>(rowoff + nrows);
-        p += (1024u - (saddr(p) & 1023u)) & 1023u;
-        tcB = reinterpret_cast<float*>(p);
-        tcA = reinterpret_cast<float*>(p + size_t(nops) * 2 * kTcBBytes);
-        tcbar = reinterpret_cast<uint64_t*>(p + size_t(nops) * 2 * kTcBBytes + 2 * kTcABytes);
-        tslot = reinterpret_cast<uint32_t*>(tcbar + 2);
-        if (warp_id() == 0) tc_alloc(tslot, kTcCols);
-    }
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) mbar_init(&mbar[b], bulk ? 1 : kTileThreads);
-        if constexpr (BLK) {
-            mbar_init(&tcbar[0], 1);
-            mbar_init(&tcbar[1], 1);
-        }
         fence_mbar_init();
         s_abort = 0;
     }
-    if constexpr (BLK) tc_fence_before();
     __syncthreads();
-    uint32_t tmem = 0, mma_parity = 0;
-    if constexpr (BLK) {
-        tc_fence_after();
-        tmem = *tslot;
-        if (threadIdx.x == 0) {  // the stage's block operands, loaded once per CTA
-            mbar_expect_tx(&tcbar[0], uint32_t(nops) * 2u * kTcBBytes);
-            for (int o = 0; o < nops; o++)
-                bulk_load(tcB + size_t(o) * 2 * kTcBBytes / 4, bfrag + sops[o].bidx, 2 * kTcBBytes, &tcbar[0]);
-        }
-        if (!mbar_wait_bounded(&tcbar[0], 0)) atomicOr(&s_abort, 1);
-        __syncthreads();
-    }
     const uint64_t first = blockIdx.x;
     const uint64_t nmy = (ntiles > first) ? (ntiles - 1 - first) / gridDim.x + 1 : 0;
     const uint32_t row_bytes = uint32_t(sizeof(GE)) << sa.RL;
@@ -493,14 +472,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
 #pragma unroll
             for (int j = 0; j < 5; j++) seg[j] = op.seg[j];
             const int kind = op.kind;
-            if (BLK) {
-                if constexpr (REP == 3 && BLK)
-                    if (kind == OP_BLOCK &&
-                        !block_apply_tc(reinterpret_cast<float*>(s), op, tcA, tcB + size_t(o) * 2 * kTcBBytes / 4,
-                                        &tcbar[1], &mma_parity, tmem))
-                        s_abort = 1;
-            } else if (REP == 3 && kind == OP_PASS) {
-                if constexpr (REP == 3 && !BLK) pass_run_c64(reinterpret_cast<float2*>(s), tsize, &base, &sops[o]);
+            if (REP == 3 && kind == OP_PASS) {
+                if constexpr (REP == 3) pass_run_c64(reinterpret_cast<float2*>(s), tsize, &base, &sops[o]);
                 o += op.k;
             } else if (kind == OP_DENSE || kind == OP_DENSE_REAL) {
                 const uint32_t tb = op.off[1];
@@ -569,12 +542,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_tile(void* __restrict__ sta
         cp_async_wait_all();  // copies of tiles the loop did not reach
         if (s_abort && threadIdx.x == 0) atomicExch(err, 1);
     }
-    if constexpr (BLK) {  // every warp is done with tensor memory: release it
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (warp_id() == 0) tc_dealloc(tmem, kTcCols);
-    }
 }
 
 static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
@@ -582,10 +549,8 @@ static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
     return e == cudaErrorMemoryAllocation ? QS_OUT_OF_MEMORY : QS_CUDA_ERROR;
 }
 
-template <int REP, bool BLK>
-static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_begin, int op_end,
-                               const TileOp* dops, const float4* dfrag, int* derr, cudaStream_t s, int sms) {
-    using E = typename TileElem<REP>::T;
+// Stage arguments shared by the tile kernels: tile geometry, copy rows and the outer expansion.
+static StageArgs stage_args(const TileStage& st, int op_begin, int op_end) {
     StageArgs sa;
     std::memset(&sa, 0, sizeof(sa));
     sa.T = st.T;
@@ -606,24 +571,161 @@ static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_b
     sa.RL = st.L + run;
     sa.RH = sa.H - run;
     for (int b = 0; b < sa.RH; b++) sa.rhigh[b] = uint8_t(st.high[run + b]);
+    return sa;
+}
+
+template <int REP>
+static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_begin, int op_end,
+                               const TileOp* dops, int* derr, cudaStream_t s, int sms) {
+    using E = typename TileElem<REP>::T;
+    StageArgs sa = stage_args(st, op_begin, op_end);
     const size_t tile_bytes = sizeof(E) << st.T;
     const size_t fixed = 4 * sizeof(uint64_t) + sizeof(TileOp) * size_t(op_end - op_begin) +
                          (sizeof(uint64_t) << sa.RH);
     sa.nbuf = (3 * tile_bytes + fixed <= 110 * 1024) ? 3 : 2;  // three buffers where two blocks still fit an SM
-    size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
-    if (BLK) {  // two tile buffers, then the resident block operands (one CTA per SM)
-        sa.nbuf = 2;
-        smem = 2 * tile_bytes + fixed + 1024 + size_t(op_end - op_begin) * 2 * kTcBBytes + 2 * kTcABytes + 32;
-    }
+    const size_t smem = size_t(sa.nbuf) * tile_bytes + fixed;
     const uint64_t ntiles = 1ull << (n - st.T);
     // One wave exactly: every CTA walks the same number of tiles, so a grid larger than what is
     // resident would leave a second, partly empty wave.
     int per_sm = 0;
-    cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile<REP, BLK>), kTileThreads, smem, &per_sm);
+    cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile<REP>), kTileThreads, smem, &per_sm);
     if (oe != cudaSuccess) return oe;
     per_sm = std::max(1, per_sm);
     const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms) * per_sm);
-    k_tile<REP, BLK><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, dfrag, derr);
+    k_tile<REP><<<int(grid), kTileThreads, smem, s>>>(state, ntiles, sa, dops, derr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) note_launches(1);
+    return e;
+}
+
+// ---- tensor-core block stages (complex64, 12-qubit tiles, only OP_BLOCK ops) ------------------
+// Two groups of kTcGroupThreads threads per CTA walk their own tiles (two tile buffers each, the
+// next tile's 16-byte pieces in flight while the current one is computed) and their own
+// tensor-memory columns; the stage's block operands are loaded once per CTA and shared. While one
+// group waits for its MMAs, the other builds its operands or moves its tiles.
+constexpr int kTcGroups = 2;
+constexpr int kTcThreads = kTcGroups * kTcGroupThreads;
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_tile_tc(float2* __restrict__ state, uint64_t ntiles,
+                                                          const __grid_constant__ StageArgs sa,
+                                                          const TileOp* __restrict__ ops,
+                                                          const float4* __restrict__ bfrag, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_tc[];
+    unsigned char* smem_raw = smem_tc;
+    const int nops = sa.op_end - sa.op_begin;
+    const uint32_t tsize = 1u << sa.T;
+    const int nrows = 1 << sa.RH;
+    // [B images, 32 KiB per op][tiles: kTcGroups x 2][index tables][ops][row offsets][mbarriers][tmem]
+    float* sB = reinterpret_cast<float*>(smem_raw);
+    float2* tiles = reinterpret_cast<float2*>(smem_raw + size_t(nops) * 2 * kTcBBytes);
+    uint32_t* tabs = reinterpret_cast<uint32_t*>(tiles + size_t(2 * kTcGroups) * tsize);
+    TileOp* sops = reinterpret_cast<TileOp*>(tabs + size_t(nops) * kTcIdxWords);
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sops + nops);
+    uint64_t* bars = rowoff + nrows;  // [0]: B copy; [1 + g]: group g's MMAs; [1 + kTcGroups + 2g + b]: tile loads
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + 3 * kTcGroups);
+    __shared__ int s_abort[kTcGroups];
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(sops);
+        const int words = nops * int(sizeof(TileOp) / 4);
+        for (int w = threadIdx.x; w < words; w += kTcThreads) dst[w] = src[w];
+    }
+    for (int r = threadIdx.x; r < nrows; r += kTcThreads) {
+        uint64_t o = 0;
+        for (int b = 0; b < sa.RH; b++)
+            if (r >> b & 1) o |= 1ull << sa.rhigh[b];
+        rowoff[r] = o;
+    }
+    if (threadIdx.x < 32) tc_alloc(tslot, kTcGroups * kTcGroupCols);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        for (int g = 0; g < kTcGroups; g++) {
+            mbar_init(&bars[1 + g], 1);
+            mbar_init(&bars[1 + kTcGroups + 2 * g], kTcGroupThreads);
+            mbar_init(&bars[2 + kTcGroups + 2 * g], kTcGroupThreads);
+            s_abort[g] = 0;
+        }
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    for (int o = 0; o < nops; o++) block_index_table(sops[o], tabs + o * kTcIdxWords, kTcThreads);
+    if (threadIdx.x == 0) {  // the stage's block operands, loaded once per CTA
+        mbar_expect_tx(&bars[0], uint32_t(nops) * 2u * kTcBBytes);
+        for (int o = 0; o < nops; o++)
+            bulk_load(sB + size_t(o) * 2 * kTcBBytes / 4, bfrag + sops[o].bidx, 2 * kTcBBytes, &bars[0]);
+    }
+    const bool b_ok = mbar_wait_bounded(&bars[0], 0);
+    __syncthreads();
+    const int g = threadIdx.x / kTcGroupThreads, gt = threadIdx.x % kTcGroupThreads;
+    const int barrier_id = 1 + g;
+    if (!b_ok && gt == 0) s_abort[g] = 1;
+    const uint64_t gid = uint64_t(blockIdx.x) * kTcGroups + uint64_t(g), ngroups = uint64_t(gridDim.x) * kTcGroups;
+    const uint64_t nmy = ntiles > gid ? (ntiles - 1 - gid) / ngroups + 1 : 0;
+    float2* gbuf = tiles + size_t(2 * g) * tsize;
+    uint64_t* lbar = &bars[1 + kTcGroups + 2 * g];
+    const uint32_t rmask = (1u << sa.RL) - 1u, pieces = tsize / 2;  // 16-byte pieces: two amplitudes
+    auto issue_load = [&](uint64_t i, int b) {
+        const uint64_t tb = expand_index(gid + i * ngroups, sa.outer);
+        float2* dst = gbuf + size_t(b) * tsize;
+        for (uint32_t c = uint32_t(gt); c < pieces; c += kTcGroupThreads) {
+            const uint32_t a = 2 * c;
+            cp_async16(dst + a, state + tb + rowoff[a >> sa.RL] + (a & rmask));
+        }
+        cp_async_mbar_arrive(&lbar[b]);
+    };
+    if (nmy > 0 && b_ok) issue_load(0, 0);
+    uint32_t lphase = 0, mma_parity = 0;
+    const uint32_t tcol = tmem + uint32_t(g) * kTcGroupCols;
+    for (uint64_t it = 0; it < nmy && b_ok; it++) {
+        const int bsel = int(it & 1);
+        if (it + 1 < nmy) issue_load(it + 1, bsel ^ 1);  // that buffer's tile was written back last iteration
+        if (!mbar_wait_bounded(&lbar[bsel], (lphase >> bsel) & 1u)) s_abort[g] = 1;
+        lphase ^= 1u << bsel;
+        named_sync(barrier_id, kTcGroupThreads);
+        if (s_abort[g]) break;
+        float* sf = reinterpret_cast<float*>(gbuf + size_t(bsel) * tsize);
+        for (int o = 0; o < nops && !s_abort[g]; o++) {
+            if (!block_apply_tc(sf, tabs + o * kTcIdxWords, sB + size_t(o) * 2 * kTcBBytes / 4, &bars[1 + g],
+                                &mma_parity, tcol, gt, barrier_id))
+                s_abort[g] = 1;
+            named_sync(barrier_id, kTcGroupThreads);
+        }
+        const uint64_t base = expand_index(gid + it * ngroups, sa.outer);
+        const float2* src = gbuf + size_t(bsel) * tsize;
+        for (uint32_t c = uint32_t(gt); c < pieces; c += kTcGroupThreads) {
+            const uint32_t a = 2 * c;
+            *reinterpret_cast<float4*>(state + base + rowoff[a >> sa.RL] + (a & rmask)) =
+                *reinterpret_cast<const float4*>(src + a);
+        }
+        named_sync(barrier_id, kTcGroupThreads);  // the buffer is free for the load two tiles ahead
+    }
+    cp_async_wait_all();  // copies of tiles the loop did not reach
+    if (gt == 0 && (s_abort[g] || !b_ok)) atomicExch(err, 1);
+    tc_fence_before();
+    __syncthreads();  // both groups are done with tensor memory
+    tc_fence_after();
+    if (threadIdx.x < 32) tc_dealloc(tmem, kTcGroups * kTcGroupCols);
+}
+
+static cudaError_t launch_tile_tc(void* state, int n, const TileStage& st, int op_begin, int op_end,
+                                  const TileOp* dops, const float4* dfrag, int* derr, cudaStream_t s, int sms) {
+    const StageArgs sa = stage_args(st, op_begin, op_end);
+    const int nops = op_end - op_begin;
+    const size_t tile_bytes = sizeof(float2) << st.T;
+    const size_t smem = size_t(nops) * 2 * kTcBBytes + size_t(2 * kTcGroups) * tile_bytes +
+                        size_t(nops) * 4 * kTcIdxWords + sizeof(TileOp) * size_t(nops) + (sizeof(uint64_t) << sa.RH) +
+                        sizeof(uint64_t) * (1 + 3 * kTcGroups) + 16;
+    const uint64_t ntiles = 1ull << (n - st.T);
+    int per_sm = 0;
+    cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile_tc), kTcThreads, smem, &per_sm);
+    if (oe != cudaSuccess) return oe;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const uint64_t groups = (ntiles + kTcGroups - 1) / kTcGroups;
+    const uint64_t grid = std::min<uint64_t>(groups, uint64_t(sms));  // one CTA per SM: its tensor memory
+    k_tile_tc<<<int(grid), kTcThreads, smem, s>>>(static_cast<float2*>(state), ntiles, sa, dops, dfrag, derr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) note_launches(1);
     return e;
@@ -702,16 +804,16 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         const int b = first[i], e2 = (i + 1 < stages.size()) ? first[i + 1] : int(host.size());
         cudaError_t e;
         switch (rep) {
-            case 0: e = launch_tile<0, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
-            case 1: e = launch_tile<1, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
-            case 2: e = launch_tile<2, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms); break;
+            case 0: e = launch_tile<0>(state, n, st, b, e2, dops, derr, s, sms); break;
+            case 1: e = launch_tile<1>(state, n, st, b, e2, dops, derr, s, sms); break;
+            case 2: e = launch_tile<2>(state, n, st, b, e2, dops, derr, s, sms); break;
             default:
                 if (dfrag)
-                    e = launch_tile<3, true>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
+                    e = launch_tile_tc(state, n, st, b, e2, dops, dfrag, derr, s, sms);
                 else if (passes[i])
                     e = launch_pass(state, n, st, b, e2, dops, derr, s, sms);
                 else
-                    e = launch_tile<3, false>(state, n, st, b, e2, dops, dfrag, derr, s, sms);
+                    e = launch_tile<3>(state, n, st, b, e2, dops, derr, s, sms);
                 break;
         }
         if (e != cudaSuccess) rc = tile_fail(e, "tile kernel", msg);
