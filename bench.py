@@ -754,10 +754,11 @@ def _measure_probs(lib, reg, target: int) -> float:
 
 def run_kernels(args) -> None:
     """A small workload that launches every kernel family once per repetition (for ncu captures):
-    init (basis and product state), dense 1-qubit (exact, FMA, DF64; complex64), CNOT/permutation,
-    dense 3-qubit, 6-qubit permutation and dense gates, probability reduction, read-back and
-    collapse (both precisions), stages (complex128 DF64 tiles, complex64 register passes, complex64
-    3xTF32 blocks), adjoint (FP64 and mixed), batch (FP64 and mixed)."""
+    init (basis and product state), dense 1-qubit (exact, FMA, DF64, fixed point; complex64),
+    CNOT/permutation, dense 3-qubit, 6-qubit permutation and dense gates, probability reduction,
+    read-back and collapse (both precisions), measurement sequences (fused collapse + next sums;
+    reference-order sums), stages (complex128 DF64 tiles, complex64 register passes, complex64 3xTF32
+    tensor-core blocks), adjoint (FP64 and mixed), batch (FP64 and mixed)."""
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
@@ -769,7 +770,7 @@ def run_kernels(args) -> None:
     haar = [g for g in layers if len(g.targets) == 1][:3]
     u3 = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0]
     for rep in range(args.steps):
-        for arith in (q.QS_ARITH_EXACT, q.QS_ARITH_FMA, q.QS_ARITH_DF64):
+        for arith in (q.QS_ARITH_EXACT, q.QS_ARITH_FMA, q.QS_ARITH_DF64, q.QS_ARITH_FX64):
             r = q.Register.from_int(n, 0)
             r.set_arith(arith)
             for g in haar:
@@ -778,6 +779,10 @@ def run_kernels(args) -> None:
         r.try_apply_fast(O.cnx([1, 2], n - 1))
         r.try_apply_fast(O.Operation(u3, [0, n // 2, n - 3]))
         r.measure(n - 1, 0.5)
+        r.measure_sequence([0, 1, n // 2], [0.3, 0.6, 0.4])  # fused collapse + next sums, live subspace
+        small = q.Register.from_int(12, 0)  # exact arithmetic: the reference's summation order
+        small.apply_gates(layers[:12] if n == 12 else flatten(layered_circuit(12, 1, 7)))
+        small.measure_sequence(list(range(12)), [0.5] * 12)
         r.apply_gates(layers, fuse=1)
         # wide gates (out-of-place kernels), a product-state register, the probability read-back
         perm = np.eye(64)[np.random.default_rng(2).permutation(64)]
