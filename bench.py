@@ -814,8 +814,9 @@ def run_case(args) -> None:
     """Small profiling workloads (for ncu captures of one kernel family, --qubits 26 by default):
     dense-<arith>: four dense 1-qubit Haar sweeps on a dense complex128 register in that arithmetic;
     blocks-c64: two layers of the family as 5-qubit 3xTF32 blocks on a complex64 register;
-    stages-c64: the same layers as register passes; measure-all: every qubit of a dense complex128
-    register measured in one sequence."""
+    blocks-fx64: the same layers as FP64-accurate 5-qubit blocks on a complex128 register (split
+    integer products on the tensor cores); stages-c64: the same layers as register passes;
+    measure-all: every qubit of a dense complex128 register measured in one sequence."""
     import quaru_gb300 as q
     from quaru_gb300.workloads import flatten, layered_circuit, seed_for
 
@@ -836,6 +837,10 @@ def run_case(args) -> None:
             r.apply_gates(ops, fuse=2, max_width=5)
         else:
             r.apply_gates(ops, fuse=1, tile_qubits=12)
+    elif args.case == "blocks-fx64":
+        r = q.Register.from_int(n, 0)
+        r.set_arith(q.QS_ARITH_FX64)
+        r.apply_gates(flatten(layered_circuit(n, 2, seed_for(3))), fuse=2, max_width=5)
     elif args.case == "measure-all":
         r = q.Register.from_int(n, 0)
         r.set_arith(q.QS_ARITH_FMA)

@@ -65,14 +65,17 @@ int apply_op(void* state, int n, int prec, int arith, const OpDesc& op, cudaStre
     return e == cudaSuccess ? QS_OK : fail(e, "wide gate", msg);
 }
 
-// fuse == 2: dense blocks of up to max_width qubits. On complex64 registers of
-// at least 12 qubits the blocks run as 3xTF32 tensor-core GEMMs inside
-// 12-qubit tiles; otherwise each block is one dense gate sweep.
+// fuse == 2: dense blocks of up to max_width qubits. On registers of at least 12 qubits, complex64
+// or complex128 in fixed-point arithmetic, the blocks run on the tensor cores inside 12-qubit
+// tiles; otherwise each block is one dense gate sweep.
 static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* gates, size_t m,
                       const qs_circuit_options& opts, cudaStream_t s, int sms, std::string* msg) {
-    const bool tensor = (prec == QS_PREC_C64) && n >= 12;
-    // automatic width: where each block's sweep stays cheap. Complex64 blocks are tensor-core GEMMs
-    // at any width up to 5; complex128 double-float blocks run the double-float dense kernel up to 3
+    // Tensor-core blocks inside 12-qubit tiles: 3xTF32 on complex64 registers; on complex128
+    // registers in fixed-point arithmetic, the FP64-accurate split-integer product (k_tile_oz).
+    const bool oz = (prec == QS_PREC_C128) && arith == QS_ARITH_FX64 && n >= 12;
+    const bool tensor = ((prec == QS_PREC_C64) && n >= 12) || oz;
+    // automatic width: where each block's sweep stays cheap. Tensor-core blocks cost the same at any
+    // width up to 5; complex128 double-float blocks run the double-float dense kernel up to 3
     // qubits (4- and 5-qubit blocks fall back to FP64, which GB300 runs at 1/64 of the FP32 rate);
     // FP64 blocks cost as many FP64 operations per amplitude as the gates they fuse, so 2 only halves
     // the sweeps.
@@ -91,9 +94,13 @@ static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* ga
             op.orig_k = 5;
             for (int j = 0; j < 5; j++) op.tq[j] = b.qubits[j];
             op.touched_rows = 32;
-            op.block = int(frags.size() / (4 * kBlockFragFloat4));
-            frags.resize(frags.size() + 4 * kBlockFragFloat4);
-            block_fragments(b.u, frags.data() + frags.size() - 4 * kBlockFragFloat4);
+            const size_t per = oz ? kOzFragBytes / 4 : 4 * kBlockFragFloat4;  // floats per block
+            op.block = int(frags.size() / per);
+            frags.resize(frags.size() + per);
+            if (oz)
+                oz_fragments(b.u, reinterpret_cast<unsigned char*>(frags.data() + frags.size() - per));
+            else
+                block_fragments(b.u, frags.data() + frags.size() - per);
         } else {
             tq.assign(b.qubits.begin(), b.qubits.end());
             classify_gate(b.u.data(), tq.size(), tq.data(), &op);
@@ -108,7 +115,7 @@ static int run_blocks(void* state, int n, int prec, int arith, const qs_gate* ga
         return QS_OK;
     }
     const int T = std::min(12, n), L = std::min(5, T);
-    std::vector<TileStage> stages = plan_tiles(ops, n, T, L, false, kMaxTcBlocks);
+    std::vector<TileStage> stages = plan_tiles(ops, n, T, L, false, oz ? kMaxOzBlocks : kMaxTcBlocks, true);
     return run_tiled(state, n, prec, arith, ops, stages, s, sms, msg, &frags);
 }
 

@@ -35,7 +35,7 @@ static uint64_t qubit_mask(const OpDesc& op) {
 static bool pure_move(const OpDesc& op) { return op.kind == OP_MONO_PF || op.kind == OP_NOOP; }
 
 std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order,
-                                  int max_ops) {
+                                  int max_ops, bool blocks_only) {
     std::vector<TileStage> stages;
     max_ops = std::max(1, std::min(max_ops, kMaxStageOps));
     if (T > n) T = n;
@@ -65,7 +65,8 @@ std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, 
             uint64_t need = 0;
             for (int j = 0; j < op.k; j++) need |= 1ull << op.tq[j];
             need &= ~low_mask;
-            if (tileable(op) && __builtin_popcountll(high | need) <= H && st.ops.size() < size_t(max_ops)) {
+            const bool fits = blocks_only ? op.kind == OP_BLOCK : tileable(op);
+            if (fits && __builtin_popcountll(high | need) <= H && st.ops.size() < size_t(max_ops)) {
                 high |= need;
                 st.ops.push_back(idx);
             } else {
@@ -144,7 +145,7 @@ TileOp make_tile_op(const OpDesc& op, const TileStage& st) {
         t.off[r] = o;
     }
     if (op.kind == OP_BLOCK) {
-        t.bidx = uint32_t(op.block) * kBlockFragFloat4;
+        t.bidx = uint32_t(op.block);
     } else if (op.kind == OP_MONO || op.kind == OP_MONO_PF) {
         for (int r = 0; r < D; r++) {
             t.offsrc[r] = t.off[op.perm[r]];

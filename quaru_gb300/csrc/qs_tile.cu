@@ -22,6 +22,7 @@
 #include "qs_device.cuh"
 #include "qs_kernels.h"
 #include "qs_tile.h"
+#include "qs_stage.h"
 #include "qs_pass.cuh"
 #include "qs_tc05.cuh"
 #include "qs_tma.cuh"
@@ -29,15 +30,6 @@
 namespace qs {
 
 constexpr int kTileThreads = 256;
-
-struct StageArgs {
-    int T, L, H;
-    int op_begin, op_end;
-    int RL, RH;            // copy rows: 2^RL contiguous amplitudes, 2^RH rows per tile
-    int nbuf;              // tile buffers in the ring (2 or 3)
-    IndexMap outer;        // expands a tile index into the base amplitude index
-    uint8_t rhigh[kTileMaxHigh];  // global qubit of row bit b
-};
 
 template <int REP>
 struct TileElem;
@@ -252,18 +244,10 @@ __device__ __forceinline__ typename TileElem<REP>::T mono_row(const TileOp& m, i
 }
 
 // ---- fused 5-qubit blocks on the tensor cores (complex64 tiles, 3xTF32)
-__device__ __forceinline__ uint32_t f2tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ uint32_t deposit5(uint32_t r, const uint8_t* pos) {
-    uint32_t o = 0;
-#pragma unroll
-    for (int b = 0; b < 5; b++) o |= ((r >> b) & 1u) << pos[b];
-    return o;
-}
+// x rounded to TF32 (10 explicit significand bits), to nearest with ties away from zero: add half
+// a TF32 unit to the magnitude bits and clear the 13 dropped bits (two integer operations; a carry
+// into the exponent field is the correct rounding up to the next binade).
+__device__ __forceinline__ uint32_t f2tf32(float x) { return (__float_as_uint(x) + 0x1000u) & 0xffffe000u; }
 
 __device__ __forceinline__ int warp_id() { return int(threadIdx.x >> 5); }
 
@@ -273,44 +257,65 @@ constexpr uint32_t kTcLbo = 128u, kTcSbo = 2048u;
 // Tensor-memory columns of one group: D (64 FP32 columns), then the A high and low parts.
 constexpr uint32_t kTcAHi = 64u, kTcALo = 128u, kTcGroupCols = 256u;
 
-// Float offsets of a block op inside the tile: column m (the 7 tile bits outside the block, 0..127)
-// starts at cof[m], block row j (0..31) adds rof[j]; the real part sits at the offset, the
-// imaginary part one float further. Built once per CTA for each block op of the stage.
-constexpr int kTcIdxWords = 128 + 32;
+// Complex64 tiles of the tensor-core stages are swizzled at 16-byte granularity (swz16, two
+// amplitudes per unit): amplitude t sits at tile_swz(t).
+__host__ __device__ __forceinline__ uint32_t tile_swz(uint32_t t) { return (swz16(t >> 1) << 1) | (t & 1u); }
+
+// Float offsets of a block op inside the swizzled tile: column m (the 7 tile bits outside the
+// block, 0..127) starts at tab[m]; block row j (0..31) XORs in tab[128 + b] (the swizzled weight of
+// block qubit b) for every set bit b of j (the swizzle is linear and the column and row bits are
+// disjoint). The real part sits at the offset, the imaginary part one float further. Built once
+// per CTA for each block op of the stage.
+constexpr int kTcIdxWords = 128 + 8;
 __device__ __forceinline__ void block_index_table(const TileOp& op, uint32_t* tab, int nthreads) {
     uint8_t pos[5];
 #pragma unroll
     for (int b = 0; b < 5; b++) pos[b] = op.pos[b];
     for (int i = threadIdx.x; i < kTcIdxWords; i += nthreads)
-        tab[i] = i < 128 ? 2u * expand_local(uint32_t(i), pos, 5) : 2u * deposit5(uint32_t(i - 128), pos);
+        tab[i] = i < 128 ? 2u * tile_swz(expand_local(uint32_t(i), pos, 5))
+                         : (i < 133 ? 2u * tile_swz(1u << pos[i - 128]) : 0u);
 }
 
 // Y = U X for the 32-row block view of a 12-qubit complex64 tile on the tensor cores (3xTF32), by
 // one group of kTcGroupThreads threads: D = A_lo B_hi + A_hi B_lo + A_hi B_hi accumulated in FP32
 // in tensor memory. A (128 x 64) holds the tile's 128 columns (the 7 tile bits outside the block)
-// by their 64 real block components (32 real parts, 32 imaginary parts), split once into TF32 high
-// and low parts and stored straight into the group's tensor-memory columns; B (64 x 64, the
-// block's [[Ur, -Ui], [Ui, Ur]]) is resident in shared memory. Warp w of the group owns tile
-// column (lane) 32 (w % 4) + lane and the real (w < 4) or imaginary (w >= 4) components. One
-// thread issues the 24 MMAs and commits them to `bar`; the group then reads D back into the tile.
-// False when the bounded wait for the MMAs gave up (the tile is left unchanged).
+// by their 64 real block components (real parts of rows 0..31 in K columns 0..31, imaginary parts
+// in 32..63), split once into TF32 high and low parts and stored straight into the group's
+// tensor-memory columns; B (64 x 64, the block's [[Ur, -Ui], [Ui, Ur]]) is resident in shared
+// memory. Warp w of the group owns tile column (lane) 32 (w % 4) + lane and block rows
+// 16 (w / 4) .. + 15, both parts (64-bit shared accesses). One thread issues the 24 MMAs and
+// commits them to `bar`; the group then reads D back into the tile. False when the bounded wait
+// for the MMAs gave up (*abort is set and the tile is left unchanged).
 constexpr int kTcGroupThreads = 256;
 __device__ __forceinline__ bool block_apply_tc(float* sf, const uint32_t* tab, const float* sb, uint64_t* bar,
-                                               uint32_t* parity, uint32_t tcol, int gt, int barrier_id) {
+                                               uint32_t* parity, uint32_t tcol, int gt, int barrier_id,
+                                               int* abort) {
     const int gw = gt >> 5, lane = gt & 31;
     const uint32_t quarter = uint32_t(gw & 3) << 21;  // lane base 32 (w % 4), in bits 16.. of the address
-    const uint32_t comp = uint32_t(gw >> 2);
-    const uint32_t col = tab[32 * (gw & 3) + lane] + comp;
-    {
-        float hi[32], lo[32];
+    const uint32_t kc = 16u * uint32_t(gw >> 2);     // this warp's rows, as K (and D) columns
+    const uint32_t col = tab[32 * (gw & 3) + lane] ^ ((gw >> 2) ? tab[132] : 0u);
+    uint32_t w[4];
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const float a = sf[col + tab[128 + j]];
-            hi[j] = __uint_as_float(f2tf32(a));
-            lo[j] = __uint_as_float(f2tf32(a - hi[j]));
+    for (int b = 0; b < 4; b++) w[b] = tab[128 + b];
+    {
+        float hre[16], him[16], lre[16], lim[16];
+        uint32_t r = col;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            if (i > 0) r ^= w[low_bit(i)];
+            const float2 a = *reinterpret_cast<const float2*>(sf + r);
+            const int j = gray_code(i);
+            hre[j] = __uint_as_float(f2tf32(a.x));
+            lre[j] = __uint_as_float(f2tf32(a.x - hre[j]));
+            him[j] = __uint_as_float(f2tf32(a.y));
+            lim[j] = __uint_as_float(f2tf32(a.y - him[j]));
         }
-        tc_st32(tcol + quarter + kTcAHi + 32u * comp, hi);
-        tc_st32(tcol + quarter + kTcALo + 32u * comp, lo);
+        const uint32_t ta = tcol + quarter + kc;
+        tc_st16_nowait(ta + kTcAHi, hre);
+        tc_st16_nowait(ta + kTcAHi + 32u, him);
+        tc_st16_nowait(ta + kTcALo, lre);
+        tc_st16_nowait(ta + kTcALo + 32u, lim);
+        tc_wait_st();
     }
     tc_fence_before();
     named_sync(barrier_id, kTcGroupThreads);
@@ -327,14 +332,25 @@ __device__ __forceinline__ bool block_apply_tc(float* sf, const uint32_t* tab, c
         }
         tc_commit(bar);
     }
-    const bool ok = mbar_wait_bounded(bar, *parity);
+    // One warp polls the barrier; the group barrier releases the other warps without spinning.
+    if (gt < 32 && !mbar_wait_bounded(bar, *parity) && gt == 0) *abort = 1;
     *parity ^= 1u;
+    tc_fence_before();
+    named_sync(barrier_id, kTcGroupThreads);
     tc_fence_after();
+    const bool ok = *abort == 0;
     if (ok) {
-        float v[32];
-        tc_ld32(tcol + quarter + 32u * comp, v);
+        uint32_t vre[16], vim[16];
+        tc_ld16_nowait(tcol + quarter + kc, vre);
+        tc_ld16_nowait(tcol + quarter + kc + 32u, vim);
+        tc_wait_ld();
+        uint32_t r = col;
 #pragma unroll
-        for (int j = 0; j < 32; j++) sf[col + tab[128 + j]] = v[j];
+        for (int i = 0; i < 16; i++) {
+            if (i > 0) r ^= w[low_bit(i)];
+            const int j = gray_code(i);
+            *reinterpret_cast<float2*>(sf + r) = make_float2(__uint_as_float(vre[j]), __uint_as_float(vim[j]));
+        }
     }
     tc_fence_before();
     named_sync(barrier_id, kTcGroupThreads);
@@ -549,31 +565,6 @@ static int tile_fail(cudaError_t e, const char* what, std::string* msg) {
     return e == cudaErrorMemoryAllocation ? QS_OUT_OF_MEMORY : QS_CUDA_ERROR;
 }
 
-// Stage arguments shared by the tile kernels: tile geometry, copy rows and the outer expansion.
-static StageArgs stage_args(const TileStage& st, int op_begin, int op_end) {
-    StageArgs sa;
-    std::memset(&sa, 0, sizeof(sa));
-    sa.T = st.T;
-    sa.L = st.L;
-    sa.H = int(st.high.size());
-    sa.op_begin = op_begin;
-    sa.op_end = op_end;
-    std::vector<int> qpos;
-    for (int q = 0; q < st.L; q++) qpos.push_back(q);
-    for (int q : st.high) qpos.push_back(q);
-    std::sort(qpos.begin(), qpos.end());
-    sa.outer.npos = int(qpos.size());
-    for (size_t i = 0; i < qpos.size(); i++) sa.outer.pos[i] = uint8_t(qpos[i]);
-    sa.outer.fixval = 0;
-    // Copy rows: high qubits L, L + 1, ... continue the contiguous low run.
-    int run = 0;
-    while (run < sa.H && st.high[run] == st.L + run) run++;
-    sa.RL = st.L + run;
-    sa.RH = sa.H - run;
-    for (int b = 0; b < sa.RH; b++) sa.rhigh[b] = uint8_t(st.high[run + b]);
-    return sa;
-}
-
 template <int REP>
 static cudaError_t launch_tile(void* state, int n, const TileStage& st, int op_begin, int op_end,
                                const TileOp* dops, int* derr, cudaStream_t s, int sms) {
@@ -655,7 +646,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_tc(float2* __restrict__ 
     if (threadIdx.x == 0) {  // the stage's block operands, loaded once per CTA
         mbar_expect_tx(&bars[0], uint32_t(nops) * 2u * kTcBBytes);
         for (int o = 0; o < nops; o++)
-            bulk_load(sB + size_t(o) * 2 * kTcBBytes / 4, bfrag + sops[o].bidx, 2 * kTcBBytes, &bars[0]);
+            bulk_load(sB + size_t(o) * 2 * kTcBBytes / 4, bfrag + size_t(sops[o].bidx) * kBlockFragFloat4,
+                      2 * kTcBBytes, &bars[0]);
     }
     const bool b_ok = mbar_wait_bounded(&bars[0], 0);
     __syncthreads();
@@ -667,12 +659,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_tc(float2* __restrict__ 
     float2* gbuf = tiles + size_t(2 * g) * tsize;
     uint64_t* lbar = &bars[1 + kTcGroups + 2 * g];
     const uint32_t rmask = (1u << sa.RL) - 1u, pieces = tsize / 2;  // 16-byte pieces: two amplitudes
+    // The pieces of this thread, 2 (gt + 256 k), share tile bits 4..8, so their swizzle is one XOR.
+    const uint32_t swz = tile_swz(2u * uint32_t(gt)) ^ (2u * uint32_t(gt));
     auto issue_load = [&](uint64_t i, int b) {
         const uint64_t tb = expand_index(gid + i * ngroups, sa.outer);
         float2* dst = gbuf + size_t(b) * tsize;
         for (uint32_t c = uint32_t(gt); c < pieces; c += kTcGroupThreads) {
             const uint32_t a = 2 * c;
-            cp_async16(dst + a, state + tb + rowoff[a >> sa.RL] + (a & rmask));
+            cp_async16(dst + (a ^ swz), state + tb + rowoff[a >> sa.RL] + (a & rmask));
         }
         cp_async_mbar_arrive(&lbar[b]);
     };
@@ -682,23 +676,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tile_tc(float2* __restrict__ 
     for (uint64_t it = 0; it < nmy && b_ok; it++) {
         const int bsel = int(it & 1);
         if (it + 1 < nmy) issue_load(it + 1, bsel ^ 1);  // that buffer's tile was written back last iteration
-        if (!mbar_wait_bounded(&lbar[bsel], (lphase >> bsel) & 1u)) s_abort[g] = 1;
+        if (gt < 32 && !mbar_wait_bounded(&lbar[bsel], (lphase >> bsel) & 1u) && gt == 0) s_abort[g] = 1;
         lphase ^= 1u << bsel;
-        named_sync(barrier_id, kTcGroupThreads);
+        named_sync(barrier_id, kTcGroupThreads);  // releases the warps that did not poll
         if (s_abort[g]) break;
         float* sf = reinterpret_cast<float*>(gbuf + size_t(bsel) * tsize);
         for (int o = 0; o < nops && !s_abort[g]; o++) {
-            if (!block_apply_tc(sf, tabs + o * kTcIdxWords, sB + size_t(o) * 2 * kTcBBytes / 4, &bars[1 + g],
-                                &mma_parity, tcol, gt, barrier_id))
-                s_abort[g] = 1;
-            named_sync(barrier_id, kTcGroupThreads);
+            block_apply_tc(sf, tabs + o * kTcIdxWords, sB + size_t(o) * 2 * kTcBBytes / 4, &bars[1 + g],
+                           &mma_parity, tcol, gt, barrier_id, &s_abort[g]);
         }
         const uint64_t base = expand_index(gid + it * ngroups, sa.outer);
         const float2* src = gbuf + size_t(bsel) * tsize;
         for (uint32_t c = uint32_t(gt); c < pieces; c += kTcGroupThreads) {
             const uint32_t a = 2 * c;
             *reinterpret_cast<float4*>(state + base + rowoff[a >> sa.RL] + (a & rmask)) =
-                *reinterpret_cast<const float4*>(src + a);
+                *reinterpret_cast<const float4*>(src + (a ^ swz));
         }
         named_sync(barrier_id, kTcGroupThreads);  // the buffer is free for the load two tiles ahead
     }
@@ -803,6 +795,11 @@ int run_tiled(void* state, int n, int prec, int arith, const std::vector<OpDesc>
         }
         const int b = first[i], e2 = (i + 1 < stages.size()) ? first[i + 1] : int(host.size());
         cudaError_t e;
+        if (dfrag && prec == QS_PREC_C128) {
+            e = launch_tile_oz(state, n, st, b, e2, dops, reinterpret_cast<const unsigned char*>(dfrag), derr, s, sms);
+            if (e != cudaSuccess) rc = tile_fail(e, "tile kernel", msg);
+            continue;
+        }
         switch (rep) {
             case 0: e = launch_tile<0>(state, n, st, b, e2, dops, derr, s, sms); break;
             case 1: e = launch_tile<1>(state, n, st, b, e2, dops, derr, s, sms); break;

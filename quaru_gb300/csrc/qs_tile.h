@@ -76,7 +76,7 @@ struct alignas(16) TileOp {
     float dfh[16];    // dense 1q double-float coefficients (see Dense1Args)
     float dfl[16];
     float mf[16];     // m rounded to float (complex64 registers)
-    uint32_t bidx;       // OP_BLOCK: offset of the block's B fragments (float4 units)
+    uint32_t bidx;       // OP_BLOCK: index of the block's operand images (each kernel knows their size)
 };
 
 // Tensor-core operand of one fused 5-qubit block: B = M, M = [[Ur, -Ui], [Ui, Ur]] (64 x 64 real,
@@ -87,6 +87,24 @@ void block_fragments(const std::vector<double>& u32x32, float* out /* 4 * kBlock
 
 // Fused blocks per tensor-core stage: the stage's B images stay resident in shared memory.
 constexpr int kMaxTcBlocks = 2;
+
+// FP64-accurate operand of one fused 5-qubit block on complex128 registers (the split-integer
+// product on the tensor cores, k_tile_oz): the block's real form B (64 x 64; input component
+// k = 2j + c, output component n = 2i + c', c = 0 real, 1 imaginary), each output column scaled by
+// its own power of two and rounded to a 55-bit integer, cut into 7 balanced base-256 digits: 7
+// BF16 slices (digit s scaled by 2^-8s) in the K-major core-matrix layout (8 KiB each); then the 64
+// output exponents (int32); then B itself in FP64, row n = output component (for amplitudes that
+// are not finite). kOzFragBytes per block.
+constexpr uint32_t kOzSliceBytes = 64u * 64u * 2u;
+constexpr int kOzSlices = 7;
+constexpr uint32_t kOzBBytes = kOzSlices * kOzSliceBytes;
+constexpr uint32_t kOzScaleBytes = 256u;
+constexpr uint32_t kOzFragBytes = kOzBBytes + kOzScaleBytes + 64u * 64u * 8u;
+void oz_fragments(const std::vector<double>& u32x32, unsigned char* out /* kOzFragBytes */);
+
+// Fused blocks per FP64-accurate tensor-core stage (the complex128 tiles take the room a second
+// block's slices would need).
+constexpr int kMaxOzBlocks = 1;
 
 struct TileStage {
     bool tiled = false;
@@ -101,9 +119,10 @@ bool tileable(const OpDesc& op);
 
 // Greedy stage planner with reordering of commuting gates (gates that share no
 // qubit). exact_order keeps arithmetic gates in their original relative order; a stage holds at most
-// max_ops (<= kMaxStageOps) gates.
+// max_ops (<= kMaxStageOps) gates. blocks_only (the tensor-core stages) admits OP_BLOCK ops only;
+// every other op runs on its own.
 std::vector<TileStage> plan_tiles(const std::vector<OpDesc>& ops, int n, int T, int L, bool exact_order,
-                                  int max_ops = kMaxStageOps);
+                                  int max_ops = kMaxStageOps, bool blocks_only = false);
 
 // Device image of one op inside `stage`.
 TileOp make_tile_op(const OpDesc& op, const TileStage& stage);
@@ -117,6 +136,11 @@ std::vector<TileOp> stage_program(const std::vector<OpDesc>& ops, const TileStag
 // variants the copy-warp pass kernel compiles (uncontrolled dense groups, swaps, uncontrolled lane
 // dense gates, lane swaps, phases); other stages run in k_tile.
 bool pass_only(const std::vector<TileOp>& prog);
+
+// Launch the FP64-accurate complex128 block kernel for one stage (dops[op_begin] is its only op,
+// an OP_BLOCK whose operand images start at frag + bidx * kOzFragBytes).
+cudaError_t launch_tile_oz(void* state, int n, const TileStage& st, int op_begin, int op_end, const TileOp* dops,
+                           const unsigned char* frag, int* derr, cudaStream_t s, int sms);
 
 // Launch the warp-specialised complex64 pass kernel for one pass-only stage whose program is
 // dops[op_begin, op_end).

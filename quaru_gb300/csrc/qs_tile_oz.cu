@@ -1,0 +1,440 @@
+// qs_tile_oz.cu — FP64-accurate fused 5-qubit blocks on complex128 registers, on the tensor cores.
+//
+// A stage applies one fused 5-qubit block U (32 x 32 complex, multiplied on the host in FP64) to
+// every 12-qubit tile of a complex128 state. In its real form the block is a 64 x 64 product
+// Y = X B per tile, X = the tile's 128 columns (the 7 tile bits outside the block) by their 64 real
+// block components. The product runs as exact integer arithmetic on the BF16 tensor cores
+// (an Ozaki-style split):
+//
+//  * every tile column m is scaled by the power of two of its largest component and rounded to a
+//    55-bit integer X (|X| <= 2^55); every output column n of B likewise, to |Y| <= 2^54 (host);
+//  * both are cut into 7 balanced base-256 digits, X = sum_s a_s 256^(6-s), Y = sum_t b_t 256^(6-t),
+//    |a_s|, |b_t| <= 128 (top digits: 128 and 64), stored as BF16 values a_s 2^-8s, b_t 2^-8t
+//    (exact: at most 8 significant bits);
+//  * tcgen05.mma kind::f16 sums the digit products in FP32 accumulators in tensor memory, one per
+//    level L = s + t for L <= 4 and one for L = 5, 6 together; the products of level L >= 7 are
+//    dropped. The level sums I_L = sum_k sum_{s+t=L} a_s b_t are integers below 2^23 for L <= 4, so
+//    those accumulators hold I_L 2^-8L exactly; the last one rounds at 2^-24 of terms below 2^-40;
+//  * R = 2^36 sum_L acc_L, assembled in 64-bit integers, is X.Y / 2^60 to within 8 units (the
+//    dropped levels cost at most 6.1, the tail's rounding and FP32 accumulation the rest); it is
+//    rounded once to double and scaled by the two powers of two.
+//
+// The error of an output is at most ulp/2 + 2^(EE-1078) sum_k |u_k| + 2^(F-55) sum_k |x_k| (the
+// operand roundings: about 2^-54 max|x| sum|u| + 2^-55 max|u| sum|x|) + 8 units of R (each below
+// 2^-46 max|x| max|u|); an FP64 FMA chain over the same 64 terms has a worst case of about
+// 2^-47 sum_k |u_k x_k|. Columns with a non-finite amplitude take an FP64 path (the block's FP64
+// real form).
+//
+// One CTA per SM (its 512 tensor-memory columns: six 64-column accumulators and two 32-column
+// slots that A slices stream through), 16 warps: warp w owns tile column 32 (w % 4) + lane (its
+// tensor-memory lane) and block rows 8 (w / 4) .. + 7 (K elements 16 (w / 4) .. + 15). While the
+// MMAs of slice s run, the warps write slice s + 1 into the other slot. One warp polls each
+// mbarrier and a CTA barrier releases the others. The next tile's 16-byte pieces load by cp.async
+// while the current tile is computed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "qs_device.cuh"
+#include "qs_kernels.h"
+#include "qs_pass.cuh"
+#include "qs_stage.h"
+#include "qs_tc05.cuh"
+#include "qs_tile.h"
+#include "qs_tma.cuh"
+
+namespace qs {
+
+namespace {
+
+constexpr int kOzThreads = 512;
+constexpr int kOzRows = 8;     // block rows per thread
+constexpr int kOzAcc = 6;                    // accumulators: levels 0..4, then 5..6
+constexpr uint32_t kOzASlot = 64u * kOzAcc;  // tensor-memory column of A slot 0 (slot 1: + 32)
+constexpr uint32_t kOzTmemCols = 512u;
+constexpr int kOzIdxWords = 128 + 8;
+constexpr long long kOzBias = 0x808080808080LL;  // X + bias: digits 1..6 are bytes - 128
+constexpr float kMagic = 12582912.0f;            // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+
+// X = round(|v| 2^(1077 - EE)) with the sign of v, for EE = max(largest exponent field of the
+// column, 1) >= v's exponent field: the significand with its implicit bit, shifted left by 2 and
+// right by EE - e with rounding to nearest (ties away from zero). |X| < 2^55.
+__device__ __forceinline__ long long oz_encode(double v, uint32_t EE) {
+    const uint32_t hi = uint32_t(__double2hiint(v)), lo = uint32_t(__double2loint(v));
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    const uint32_t d = min(EE - max(e, 1u), 63u);
+    // 2m = significand << 3 (< 2^56); X = ((2m >> d) + 1) >> 1 rounds m / 2^d to nearest
+    const uint64_t m2 = ((uint64_t((hi & 0xfffffu) | (e != 0u ? 0x100000u : 0u)) << 32) | lo) << 3;
+    const uint64_t X = ((m2 >> d) + 1u) >> 1;
+    const long long sg = (long long)(int32_t(hi) >> 31);  // 0 or -1
+    return ((long long)X ^ sg) - sg;
+}
+
+// Digit s of Xb = X + kOzBias as a float, scaled by 2^-8s (s = 0: the signed top part Xb >> 48;
+// s >= 1: byte 6 - s minus 128, placed under the float 2^(23-8s) by a byte permute and recovered
+// by one exact subtraction).
+template <int S>
+__device__ __forceinline__ uint32_t oz_digit_bits(long long Xb) {
+    if constexpr (S == 0) {
+        const int d = int(uint32_t(uint64_t(Xb) >> 32)) >> 16;
+        return __float_as_uint(__int_as_float(kMagicBits + d) - kMagic);
+    } else {
+        constexpr int i = 6 - S;
+        constexpr uint32_t magic = uint32_t(150 - 8 * S) << 23;  // 2^(23 - 8 S)
+        const uint32_t word = i < 4 ? uint32_t(uint64_t(Xb)) : uint32_t(uint64_t(Xb) >> 32);
+        const uint32_t bits = __byte_perm(word, magic, 0x7650u | uint32_t(i & 3));
+        return __float_as_uint(__uint_as_float(bits) - __uint_as_float(magic | 0x80u));
+    }
+}
+
+// Slice S of the thread's 16 K elements (row r: real part at 2r, imaginary at 2r + 1), packed as
+// BF16 pairs (element 2c in the low half of column c).
+template <int S>
+__device__ __forceinline__ void oz_slice(const long long (&X)[2 * kOzRows], uint32_t (&pk)[kOzRows]) {
+#pragma unroll
+    for (int c = 0; c < kOzRows; c++)
+        pk[c] = __byte_perm(oz_digit_bits<S>(X[2 * c]), oz_digit_bits<S>(X[2 * c + 1]), 0x7632u);
+}
+
+// R = 2^36 (acc_0 + ... + acc_5) as an integer: levels 0..3 through the magic-number conversion
+// (|I_L| < 2^22), level 4 by a rounding conversion (|I_4| < 2^23), the tail rounded at 2^-36.
+__device__ __forceinline__ long long oz_combine(float a0, float a1, float a2, float a3, float a4, float a5) {
+    const int i0 = __float_as_int(a0 + kMagic) - kMagicBits;
+    const int i1 = __float_as_int(fmaf(a1, 256.0f, kMagic)) - kMagicBits;
+    const int i2 = __float_as_int(fmaf(a2, 65536.0f, kMagic)) - kMagicBits;
+    const int i3 = __float_as_int(fmaf(a3, 16777216.0f, kMagic)) - kMagicBits;
+    const int i4 = __float2int_rn(a4 * 4294967296.0f);
+    const int t = __float_as_int(fmaf(a5, 68719476736.0f, kMagic)) - kMagicBits;
+    const int j01 = i0 * 256 + i1, j23 = i2 * 256 + i3;  // below 2^28 and 2^30
+    return ((long long)j01 << 28) + ((long long)j23 << 12) + ((long long)i4 << 4) + (long long)t;
+}
+
+__device__ __forceinline__ double oz_to_double(long long R, int k) {
+    return (k >= kFxFastKMin && k <= kFxFastKMax) ? fx_to_double_fast(R, k << 20) : fx_to_double_any(R, k);
+}
+
+// Amplitude offset (16-byte units, swizzled) of block row j of this thread's column.
+__device__ __forceinline__ uint32_t oz_row(uint32_t col0, const uint32_t* tab, int j) {
+    uint32_t r = col0;
+#pragma unroll
+    for (int b = 0; b < 5; b++)
+        if (j >> b & 1) r ^= tab[128 + b];
+    return r;
+}
+
+// Columns with a non-finite amplitude: the thread's 16 outputs in FP64 from the column's 64 inputs
+// (all four row groups, read from the tile before any result is written) and the block's FP64
+// real form. Rolled loops, so the common path keeps its registers.
+__device__ __forceinline__ void oz_rare_column(const double2* tl, const uint32_t* tab, int m, int g, const double* bd,
+                                               double* out) {
+#pragma unroll 1
+    for (int q = 0; q < 2 * kOzRows; q++) {
+        const int nidx = 2 * kOzRows * g + q;
+        double acc = 0.0;
+#pragma unroll 1
+        for (int j = 0; j < 32; j++) {
+            const double2 v = tl[oz_row(tab[m], tab, j)];
+            acc = fma(bd[nidx * 64 + 2 * j], v.x, acc);
+            acc = fma(bd[nidx * 64 + 2 * j + 1], v.y, acc);
+        }
+        out[q] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1)
+    k_tile_oz(double2* __restrict__ state, uint64_t ntiles, const __grid_constant__ StageArgs sa,
+              const TileOp* __restrict__ ops, const unsigned char* __restrict__ frag, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_oz[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t tsize = 1u << sa.T;
+    const int nrows = 1 << sa.RH;
+    // [B slices][output exponents][tiles x 2][index table][op][row offsets][exponent exchange][bars][tmem]
+    unsigned char* sB = smem_oz;
+    const int* sscale = reinterpret_cast<const int*>(smem_oz + kOzBBytes);
+    double2* tiles = reinterpret_cast<double2*>(smem_oz + kOzBBytes + kOzScaleBytes);
+    uint32_t* tab = reinterpret_cast<uint32_t*>(tiles + 2 * size_t(tsize));
+    TileOp* sop = reinterpret_cast<TileOp*>(tab + kOzIdxWords);
+    uint64_t* rowoff = reinterpret_cast<uint64_t*>(sop + 1);
+    uint32_t* ex = reinterpret_cast<uint32_t*>(rowoff + nrows);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ex + 512);  // [0] operands, [1..2] A slots, [3..4] tile loads
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    __shared__ int s_abort;
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(sop);
+        for (int w = tid; w < int(sizeof(TileOp) / 4); w += kOzThreads) dst[w] = src[w];
+    }
+    for (int r = tid; r < nrows; r += kOzThreads) {
+        uint64_t o = 0;
+        for (int b = 0; b < sa.RH; b++)
+            if (r >> b & 1) o |= 1ull << sa.rhigh[b];
+        rowoff[r] = o;
+    }
+    if (warp == 0) tc_alloc(tslot, kOzTmemCols);
+    if (tid == 0) {
+        for (int b = 0; b < 3; b++) mbar_init(&bars[b], 1);
+        mbar_init(&bars[3], kOzThreads);
+        mbar_init(&bars[4], kOzThreads);
+        fence_mbar_init();
+        s_abort = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    {
+        uint8_t pos[5];
+#pragma unroll
+        for (int b = 0; b < 5; b++) pos[b] = sop->pos[b];
+        for (int i = tid; i < kOzIdxWords; i += kOzThreads)
+            tab[i] = i < 128 ? swz16(expand_local(uint32_t(i), pos, 5)) : (i < 133 ? swz16(1u << pos[i - 128]) : 0u);
+    }
+    const unsigned char* bfrag = frag + size_t(sop->bidx) * kOzFragBytes;
+    if (tid == 0) {  // the block's slices and output exponents, once per CTA
+        mbar_expect_tx(&bars[0], kOzBBytes + kOzScaleBytes);
+        for (int s = 0; s < kOzSlices; s++)
+            bulk_load(sB + s * kOzSliceBytes, bfrag + s * kOzSliceBytes, kOzSliceBytes, &bars[0]);
+        bulk_load(sB + kOzBBytes, bfrag + kOzBBytes, kOzScaleBytes, &bars[0]);
+    }
+    if (warp == 0 && !mbar_wait_bounded(&bars[0], 0) && lane == 0) s_abort = 1;
+    __syncthreads();
+    const double* bd = reinterpret_cast<const double*>(bfrag + kOzBBytes + kOzScaleBytes);
+
+    const uint64_t first = blockIdx.x, stride = gridDim.x;
+    const uint64_t nmy = ntiles > first ? (ntiles - 1 - first) / stride + 1 : 0;
+    const uint32_t rmask = (1u << sa.RL) - 1u;
+    // The pieces of this thread, tid + 512 k, share unit bits 3..7, so their swizzle is one XOR.
+    const uint32_t swz = swz16(uint32_t(tid)) ^ uint32_t(tid);
+    auto issue_load = [&](uint64_t i, int b) {
+        const uint64_t tb = expand_index(first + i * stride, sa.outer);
+        double2* dst = tiles + size_t(b) * tsize;
+        for (uint32_t c = uint32_t(tid); c < tsize; c += kOzThreads)
+            cp_async16(dst + (c ^ swz), state + tb + rowoff[c >> sa.RL] + (c & rmask));
+        cp_async_mbar_arrive(&bars[3 + b]);
+    };
+    if (nmy > 0 && !s_abort) issue_load(0, 0);
+
+    const int q = warp & 3, g = warp >> 2, m = 32 * q + lane;  // row group g: block rows 8 g .. 8 g + 7
+    const uint32_t quarter = uint32_t(32 * q) << 16;
+    const uint32_t col0 = tab[m] ^ ((g & 1) ? tab[131] : 0u) ^ ((g & 2) ? tab[132] : 0u);  // row 8 g
+    uint32_t w[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) w[b] = tab[128 + b];
+    constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
+    const uint32_t sb0 = saddr(sB);
+    uint32_t lph = 0, ph1 = 0, ph2 = 0;  // tile-load phases (bit b); A-slot barrier phases
+    // Warp 0 waits until the MMAs that read A slot `slot` last have completed; the CTA barrier that
+    // follows every call releases the other warps.
+    auto slot_wait = [&](int slot) {
+        uint32_t& ph = slot ? ph2 : ph1;
+        if (warp == 0 && !s_abort && !mbar_wait_bounded(&bars[1 + slot], ph & 1u) && lane == 0) s_abort = 1;
+        ph++;
+    };
+    auto issue_mma = [&](int s) {  // slice s against every B slice t with s + t <= 6
+        const uint32_t aslot = tmem + kOzASlot + 32u * uint32_t(s & 1);
+#pragma unroll
+        for (int t = 0; t < kOzSlices; t++) {
+            if (s + t >= kOzSlices) break;
+            const uint32_t acc = tmem + 64u * uint32_t(min(s + t, kOzAcc - 1));
+            const uint32_t bs = sb0 + uint32_t(t) * kOzSliceBytes;
+#pragma unroll
+            for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
+                tc_mma_f16_ta(acc, aslot + 8u * ks, tc_smem_desc(bs + 256u * ks, 128u, 1024u), idesc,
+                              (s > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
+        }
+        tc_commit(&bars[1 + (s & 1)]);
+    };
+    double rare_out[2 * kOzRows];
+
+    for (uint64_t it = 0; it < nmy; it++) {
+        const int b = int(it & 1);
+        if (it + 1 < nmy) issue_load(it + 1, b ^ 1);  // that buffer's tile was written back last iteration
+        if (warp == 0 && !mbar_wait_bounded(&bars[3 + b], (lph >> b) & 1u) && lane == 0) s_abort = 1;
+        lph ^= 1u << b;
+        __syncthreads();  // releases the warps that did not poll
+        if (s_abort) break;
+        double2* tl = tiles + size_t(b) * tsize;
+
+        // this thread's 8 amplitudes, the column's exponent
+        long long X[2 * kOzRows];
+        uint32_t emax = 0;
+        {
+            double2 v[kOzRows];
+            uint32_t r = col0;
+#pragma unroll
+            for (int i = 0; i < kOzRows; i++) {
+                if (i > 0) r ^= w[low_bit(i)];
+                v[gray_code(i)] = tl[r];
+            }
+#pragma unroll
+            for (int j = 0; j < kOzRows; j++) emax = max(emax, max(fx_efield(v[j].x), fx_efield(v[j].y)));
+            ex[g * 128 + m] = emax;
+            __syncthreads();
+            emax = max(max(ex[m], ex[128 + m]), max(ex[256 + m], ex[384 + m]));
+            const uint32_t EE = max(emax, 1u);
+            const bool fin = emax != 0x7ffu;
+#pragma unroll
+            for (int j = 0; j < kOzRows; j++) {
+                X[2 * j] = (fin ? oz_encode(v[j].x, EE) : 0ll) + kOzBias;
+                X[2 * j + 1] = (fin ? oz_encode(v[j].y, EE) : 0ll) + kOzBias;
+            }
+        }
+        const bool rare = emax == 0x7ffu;
+
+        // slices 0..6 through the two A slots
+        const uint32_t ta = tmem + quarter + kOzASlot + uint32_t(kOzRows * g);
+        auto put = [&](int s, const uint32_t (&pk)[kOzRows]) {
+            if (s >= 2) {
+                slot_wait(s & 1);
+                __syncthreads();
+            }
+            tc_fence_after();
+            tc_st8u_nowait(ta + 32u * uint32_t(s & 1), pk);
+            tc_wait_st();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0 && !s_abort) issue_mma(s);
+        };
+        {
+            uint32_t pk[kOzRows];
+            oz_slice<0>(X, pk);
+            put(0, pk);
+            oz_slice<1>(X, pk);
+            put(1, pk);
+            oz_slice<2>(X, pk);
+            put(2, pk);
+            oz_slice<3>(X, pk);
+            put(3, pk);
+            oz_slice<4>(X, pk);
+            put(4, pk);
+            oz_slice<5>(X, pk);
+            put(5, pk);
+            oz_slice<6>(X, pk);
+            put(6, pk);
+        }
+        // columns with a non-finite amplitude: FP64 results from the tile, which no thread has written yet
+        if (rare) oz_rare_column(tl, tab, m, g, bd, rare_out);
+        slot_wait(1);  // slice 5
+        slot_wait(0);  // slice 6: every MMA of the tile has completed
+        if (__syncthreads_or(s_abort)) break;  // a wait gave up: leave the tile unwritten
+        tc_fence_after();
+
+        // R -> double for the thread's 8 rows (D columns 16 g .. + 15: row 8 g + i, real then imaginary)
+        const int kE = int(max(emax, 1u));
+#pragma unroll
+        for (int r2 = 0; r2 < kOzRows / 2; r2++) {  // two rows (four D columns) at a time
+            uint32_t a[kOzAcc][4];
+#pragma unroll
+            for (int L = 0; L < kOzAcc; L++)
+                tc_ld4_nowait(tmem + quarter + 64u * L + uint32_t(2 * kOzRows * g) + 4u * r2, a[L]);
+            tc_wait_ld();
+#pragma unroll
+            for (int e = 0; e < 4; e += 2) {
+                const int i = 2 * r2 + e / 2;  // row 8 g + i
+                double2 y;
+                if (!rare) {
+                    const int n0 = 2 * kOzRows * g + 4 * r2 + e;
+                    const long long R0 = oz_combine(__uint_as_float(a[0][e]), __uint_as_float(a[1][e]),
+                                                    __uint_as_float(a[2][e]), __uint_as_float(a[3][e]),
+                                                    __uint_as_float(a[4][e]), __uint_as_float(a[5][e]));
+                    const long long R1 = oz_combine(__uint_as_float(a[0][e + 1]), __uint_as_float(a[1][e + 1]),
+                                                    __uint_as_float(a[2][e + 1]), __uint_as_float(a[3][e + 1]),
+                                                    __uint_as_float(a[4][e + 1]), __uint_as_float(a[5][e + 1]));
+                    y.x = oz_to_double(R0, kE + sscale[n0]);
+                    y.y = oz_to_double(R1, kE + sscale[n0 + 1]);
+                } else {
+                    y.x = rare_out[2 * i];
+                    y.y = rare_out[2 * i + 1];
+                }
+                tl[oz_row(col0, tab, i)] = y;  // row 8 g + i: bits of i over tab[128..130]
+            }
+        }
+        tc_fence_before();
+        __syncthreads();  // the tile is complete; the accumulators are free for the next tile
+        tc_fence_after();
+        const uint64_t base = expand_index(first + it * stride, sa.outer);
+        for (uint32_t c = uint32_t(tid); c < tsize; c += kOzThreads)
+            state[base + rowoff[c >> sa.RL] + (c & rmask)] = tl[c ^ swz];
+        __syncthreads();  // the buffer is free for the load two tiles ahead
+    }
+    cp_async_wait_all();  // copies of tiles the loop did not reach
+    if (tid == 0 && s_abort) atomicExch(err, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tc_dealloc(tmem, kOzTmemCols);
+}
+
+}  // namespace
+
+cudaError_t launch_tile_oz(void* state, int n, const TileStage& st, int op_begin, int op_end, const TileOp* dops,
+                           const unsigned char* frag, int* derr, cudaStream_t s, int sms) {
+    if (op_end - op_begin != 1 || st.T != 12) return cudaErrorInvalidValue;
+    const StageArgs sa = stage_args(st, op_begin, op_end);
+    const size_t tile_bytes = sizeof(double2) << st.T;
+    const size_t smem = kOzBBytes + kOzScaleBytes + 2 * tile_bytes + 4 * size_t(kOzIdxWords) + sizeof(TileOp) +
+                        (sizeof(uint64_t) << sa.RH) + 512 * 4 + 5 * sizeof(uint64_t) + 16;
+    const uint64_t ntiles = 1ull << (n - st.T);
+    int per_sm = 0;
+    cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile_oz), kOzThreads, smem, &per_sm);
+    if (oe != cudaSuccess) return oe;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const uint64_t grid = std::min<uint64_t>(ntiles, uint64_t(sms));  // one CTA per SM: its tensor memory
+    k_tile_oz<<<int(grid), kOzThreads, smem, s>>>(static_cast<double2*>(state), ntiles, sa, dops, frag, derr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) note_launches(1);
+    return e;
+}
+
+// Balanced base-256 digits of Y (|Y| <= 2^54), most significant first: Y = sum_t d[t] 256^(6-t).
+static void oz_digits(long long Y, int (&d)[kOzSlices]) {
+    const long long Yb = Y + kOzBias;
+    for (int i = 0; i < 6; i++) d[6 - i] = int((Yb >> (8 * i)) & 255) - 128;
+    d[0] = int(Yb >> 48);
+}
+
+static uint16_t bf16_exact(double v) {  // v has at most 8 significant bits
+    const float f = float(v);
+    uint32_t bits;
+    std::memcpy(&bits, &f, 4);
+    return uint16_t(bits >> 16);
+}
+
+void oz_fragments(const std::vector<double>& u, unsigned char* out) {
+    // real form: input component k = 2j + c, output component n = 2i + c'
+    auto B = [&](int n, int k) -> double {
+        const int i = n >> 1, j = k >> 1;
+        const double re = u[2 * (i * 32 + j)], im = u[2 * (i * 32 + j) + 1];
+        const bool out_im = n & 1, in_im = k & 1;
+        if (out_im == in_im) return re;
+        return out_im ? im : -im;  // yi += Ui xr; yr -= Ui xi
+    };
+    std::memset(out, 0, kOzFragBytes);
+    int32_t* scale = reinterpret_cast<int32_t*>(out + kOzBBytes);
+    double* bd = reinterpret_cast<double*>(out + kOzBBytes + kOzScaleBytes);
+    for (int n = 0; n < 64; n++) {
+        double mx = 0.0;
+        for (int k = 0; k < 64; k++) mx = std::max(mx, std::fabs(B(n, k)));
+        int F = 0;
+        if (mx > 0.0) std::frexp(mx, &F);
+        scale[n] = F - 1071;
+        for (int k = 0; k < 64; k++) {
+            const double v = B(n, k);
+            bd[n * 64 + k] = v;
+            const long long Y = std::llrint(std::ldexp(v, 54 - F));
+            int d[kOzSlices];
+            oz_digits(Y, d);
+            for (int t = 0; t < kOzSlices; t++) {
+                const uint16_t h = bf16_exact(std::ldexp(double(d[t]), -8 * t));
+                std::memcpy(out + t * kOzSliceBytes + tc_kmajor_off16(uint32_t(n), uint32_t(k), 8u), &h, 2);
+            }
+        }
+    }
+}
+
+}  // namespace qs
