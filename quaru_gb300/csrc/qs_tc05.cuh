@@ -147,6 +147,9 @@ __device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]
         : "r"(taddr)
         : "memory");
 }
+__device__ __forceinline__ void tc_ld2_nowait(uint32_t taddr, uint32_t (&r)[2]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr) : "memory");
+}
 __device__ __forceinline__ void tc_ld4_nowait(uint32_t taddr, uint32_t (&r)[4]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])

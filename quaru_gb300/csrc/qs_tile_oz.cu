@@ -25,12 +25,21 @@
 // 2^-47 sum_k |u_k x_k|. Columns with a non-finite amplitude take an FP64 path (the block's FP64
 // real form).
 //
-// One CTA per SM (its 512 tensor-memory columns: six 64-column accumulators and two 32-column
-// slots that A slices stream through), 16 warps: warp w owns tile column 32 (w % 4) + lane (its
-// tensor-memory lane) and block rows 8 (w / 4) .. + 7 (K elements 16 (w / 4) .. + 15). While the
-// MMAs of slice s run, the warps write slice s + 1 into the other slot. One warp polls each
-// mbarrier and a CTA barrier releases the others. The next tile's 16-byte pieces load by cp.async
-// while the current tile is computed.
+// One CTA per SM (its 512 tensor-memory columns: six 64-column accumulators and four 32-column
+// slots that A slices stream through) runs a warp-specialised pipeline over its tiles:
+//  * 16 math warps: warp w owns tile column 32 (w % 4) + lane (its tensor-memory lane) and block
+//    rows 8 (w / 4) .. + 7 (K elements 16 (w / 4) .. + 15). Per tile they encode the column, write
+//    its 7 slices into the slots (each slot handed over by an mbarrier: "full" when the 16 warps
+//    have stored it, "free" when the MMAs that read it have completed), drain the previous tile's
+//    accumulators into 64-bit integers while the current tile's first slices wait, and finish the
+//    previous tile (rounding, scaling, stores straight from registers to the state) while the
+//    current tile's MMAs run;
+//  * one MMA warp: one thread issues each slice's MMAs as soon as the slice is stored (and, for a
+//    tile's first slice, the previous tile's accumulators are drained) and commits them to the
+//    slot's "free" barrier and, after the last slice, to "accumulators full".
+// A tile is loaded by 16-byte cp.async pieces into one of two buffers one tile ahead; the only
+// barrier among the math warps per tile is the exchange of the column exponents, which also marks
+// the moment every read of the older buffer is done. Every wait is bounded.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,12 +59,19 @@ namespace qs {
 
 namespace {
 
-constexpr int kOzThreads = 512;
-constexpr int kOzRows = 8;     // block rows per thread
+constexpr int kOzMathWarps = 16;
+constexpr int kOzMath = 32 * kOzMathWarps;   // math threads; the MMA warp follows them
+constexpr int kOzThreads = kOzMath + 32;
+constexpr int kOzRows = 8;                   // block rows per math thread
 constexpr int kOzAcc = 6;                    // accumulators: levels 0..4, then 5..6
-constexpr uint32_t kOzASlot = 64u * kOzAcc;  // tensor-memory column of A slot 0 (slot 1: + 32)
+constexpr int kOzSlots = 4;                  // A slots in tensor memory
+constexpr uint32_t kOzASlot = 64u * kOzAcc;  // tensor-memory column of A slot 0 (slot j: + 32 j)
 constexpr uint32_t kOzTmemCols = 512u;
-constexpr int kOzIdxWords = 128 + 8;
+constexpr int kOzIdxWords = 128 + 16;
+// mbarriers: B operand, tile loads (2), slot full (4), slot free (4), accumulators full / drained,
+// final MMA completion
+constexpr int kBarB = 0, kBarLoad = 1, kBarFull = 3, kBarFree = 7, kBarAccFull = 11, kBarAccFree = 12,
+              kBarDone = 13, kOzBars = 14;
 constexpr long long kOzBias = 0x808080808080LL;  // X + bias: digits 1..6 are bytes - 128
 constexpr float kMagic = 12582912.0f;            // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
@@ -126,22 +142,44 @@ __device__ __forceinline__ uint32_t oz_row(uint32_t col0, const uint32_t* tab, i
     return r;
 }
 
+// Barrier among the 16 math warps (hardware barrier 1) that also ORs `flag` over them.
+__device__ __forceinline__ bool math_sync_or(bool flag) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"(uint32_t(flag)), "n"(kOzMath)
+        : "memory");
+    return r != 0;
+}
+
 // Columns with a non-finite amplitude: the thread's 16 outputs in FP64 from the column's 64 inputs
-// (all four row groups, read from the tile before any result is written) and the block's FP64
-// real form. Rolled loops, so the common path keeps its registers.
-__device__ __forceinline__ void oz_rare_column(const double2* tl, const uint32_t* tab, int m, int g, const double* bd,
-                                               double* out) {
+// (all four row groups, read from the tile buffer, which no load refills before the next tile's
+// exponent exchange) and the block's FP64 real form, stored straight to the state (dst = the
+// tile's base). Rolled loops, so the common path keeps its registers.
+__device__ __noinline__ void oz_rare_column(const double2* tl, const uint32_t* tab, int m, int g, const double* bd,
+                                            double2* dst, const uint64_t* rowoff, uint32_t rmask, int RL,
+                                            uint32_t lrow0) {
 #pragma unroll 1
-    for (int q = 0; q < 2 * kOzRows; q++) {
-        const int nidx = 2 * kOzRows * g + q;
-        double acc = 0.0;
+    for (int i = 0; i < kOzRows; i++) {
+        double y[2];
 #pragma unroll 1
-        for (int j = 0; j < 32; j++) {
-            const double2 v = tl[oz_row(tab[m], tab, j)];
-            acc = fma(bd[nidx * 64 + 2 * j], v.x, acc);
-            acc = fma(bd[nidx * 64 + 2 * j + 1], v.y, acc);
+        for (int c = 0; c < 2; c++) {
+            const int nidx = 2 * (kOzRows * g + i) + c;
+            double acc = 0.0;
+#pragma unroll 1
+            for (int j = 0; j < 32; j++) {
+                const double2 v = tl[oz_row(tab[m], tab, j)];
+                acc = fma(bd[nidx * 64 + 2 * j], v.x, acc);
+                acc = fma(bd[nidx * 64 + 2 * j + 1], v.y, acc);
+            }
+            y[c] = acc;
         }
-        out[q] = acc;
+        uint32_t l = lrow0;
+#pragma unroll 1
+        for (int b = 0; b < 3; b++)
+            if (i >> b & 1) l ^= tab[136 + b];
+        dst[rowoff[l >> RL] + (l & rmask)] = make_double2(y[0], y[1]);
     }
 }
 
@@ -152,7 +190,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t tsize = 1u << sa.T;
     const int nrows = 1 << sa.RH;
-    // [B slices][output exponents][tiles x 2][index table][op][row offsets][exponent exchange][bars][tmem]
+    // [B slices][output exponents][tiles x 2][index table][op][row offsets][exponents x 2][bars][tmem]
     unsigned char* sB = smem_oz;
     const int* sscale = reinterpret_cast<const int*>(smem_oz + kOzBBytes);
     double2* tiles = reinterpret_cast<double2*>(smem_oz + kOzBBytes + kOzScaleBytes);
@@ -160,8 +198,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     TileOp* sop = reinterpret_cast<TileOp*>(tab + kOzIdxWords);
     uint64_t* rowoff = reinterpret_cast<uint64_t*>(sop + 1);
     uint32_t* ex = reinterpret_cast<uint32_t*>(rowoff + nrows);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(ex + 512);  // [0] operands, [1..2] A slots, [3..4] tile loads
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(ex + 2 * kOzMath);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kOzBars);
     __shared__ int s_abort;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
@@ -174,11 +212,17 @@ __global__ void __launch_bounds__(kOzThreads, 1)
             if (r >> b & 1) o |= 1ull << sa.rhigh[b];
         rowoff[r] = o;
     }
-    if (warp == 0) tc_alloc(tslot, kOzTmemCols);
+    if (warp == kOzMathWarps) tc_alloc(tslot, kOzTmemCols);
     if (tid == 0) {
-        for (int b = 0; b < 3; b++) mbar_init(&bars[b], 1);
-        mbar_init(&bars[3], kOzThreads);
-        mbar_init(&bars[4], kOzThreads);
+        mbar_init(&bars[kBarB], 1);
+        for (int b = 0; b < 2; b++) mbar_init(&bars[kBarLoad + b], kOzMath);
+        for (int j = 0; j < kOzSlots; j++) {
+            mbar_init(&bars[kBarFull + j], kOzMathWarps);
+            mbar_init(&bars[kBarFree + j], 1);
+        }
+        mbar_init(&bars[kBarAccFull], 1);
+        mbar_init(&bars[kBarAccFree], kOzMathWarps);
+        mbar_init(&bars[kBarDone], 1);
         fence_mbar_init();
         s_abort = 0;
     }
@@ -187,187 +231,231 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     tc_fence_after();
     const uint32_t tmem = *tslot;
     {
+        // [0, 128): swizzled tile unit of column i's row 0; [128, 133): swizzled unit offset of block
+        // qubit b; [136, 141): the same offsets unswizzled (tile-local amplitude bits)
         uint8_t pos[5];
 #pragma unroll
         for (int b = 0; b < 5; b++) pos[b] = sop->pos[b];
         for (int i = tid; i < kOzIdxWords; i += kOzThreads)
-            tab[i] = i < 128 ? swz16(expand_local(uint32_t(i), pos, 5)) : (i < 133 ? swz16(1u << pos[i - 128]) : 0u);
+            tab[i] = i < 128   ? swz16(expand_local(uint32_t(i), pos, 5))
+                     : i < 133 ? swz16(1u << pos[i - 128])
+                     : (i >= 136 && i < 141) ? (1u << pos[i - 136])
+                                             : 0u;
     }
     const unsigned char* bfrag = frag + size_t(sop->bidx) * kOzFragBytes;
     if (tid == 0) {  // the block's slices and output exponents, once per CTA
-        mbar_expect_tx(&bars[0], kOzBBytes + kOzScaleBytes);
+        mbar_expect_tx(&bars[kBarB], kOzBBytes + kOzScaleBytes);
         for (int s = 0; s < kOzSlices; s++)
-            bulk_load(sB + s * kOzSliceBytes, bfrag + s * kOzSliceBytes, kOzSliceBytes, &bars[0]);
-        bulk_load(sB + kOzBBytes, bfrag + kOzBBytes, kOzScaleBytes, &bars[0]);
+            bulk_load(sB + s * kOzSliceBytes, bfrag + s * kOzSliceBytes, kOzSliceBytes, &bars[kBarB]);
+        bulk_load(sB + kOzBBytes, bfrag + kOzBBytes, kOzScaleBytes, &bars[kBarB]);
     }
-    if (warp == 0 && !mbar_wait_bounded(&bars[0], 0) && lane == 0) s_abort = 1;
+    if (warp == 0 && !mbar_wait_bounded(&bars[kBarB], 0) && lane == 0) s_abort = 1;
     __syncthreads();
     const double* bd = reinterpret_cast<const double*>(bfrag + kOzBBytes + kOzScaleBytes);
 
     const uint64_t first = blockIdx.x, stride = gridDim.x;
     const uint64_t nmy = ntiles > first ? (ntiles - 1 - first) / stride + 1 : 0;
     const uint32_t rmask = (1u << sa.RL) - 1u;
-    // The pieces of this thread, tid + 512 k, share unit bits 3..7, so their swizzle is one XOR.
-    const uint32_t swz = swz16(uint32_t(tid)) ^ uint32_t(tid);
-    auto issue_load = [&](uint64_t i, int b) {
-        const uint64_t tb = expand_index(first + i * stride, sa.outer);
-        double2* dst = tiles + size_t(b) * tsize;
-        for (uint32_t c = uint32_t(tid); c < tsize; c += kOzThreads)
-            cp_async16(dst + (c ^ swz), state + tb + rowoff[c >> sa.RL] + (c & rmask));
-        cp_async_mbar_arrive(&bars[3 + b]);
-    };
-    if (nmy > 0 && !s_abort) issue_load(0, 0);
 
-    const int q = warp & 3, g = warp >> 2, m = 32 * q + lane;  // row group g: block rows 8 g .. 8 g + 7
-    const uint32_t quarter = uint32_t(32 * q) << 16;
-    const uint32_t col0 = tab[m] ^ ((g & 1) ? tab[131] : 0u) ^ ((g & 2) ? tab[132] : 0u);  // row 8 g
-    uint32_t w[3];
+    if (warp == kOzMathWarps) {
+        // ---- the MMA warp: slice s of a tile against every B slice t with s + t <= 6
+        if (lane == 0) {
+            bool ok = s_abort == 0;
+            constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
+            const uint32_t sb0 = saddr(sB);
+            for (uint64_t it = 0; ok && it < nmy; it++) {
+                for (int s = 0; s < kOzSlices; s++) {
+                    const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
+                    const uint32_t slot = uint32_t(u & 3u);
+                    if (!mbar_wait_bounded(&bars[kBarFull + slot], uint32_t((u >> 2) & 1u))) {
+                        ok = false;
+                        break;
+                    }
+                    // a tile's first MMAs overwrite the accumulators: the previous tile's must be drained
+                    if (s == 0 && it > 0 && !mbar_wait_bounded(&bars[kBarAccFree], uint32_t((it - 1) & 1u))) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t aslot = tmem + kOzASlot + 32u * slot;
 #pragma unroll
-    for (int b = 0; b < 3; b++) w[b] = tab[128 + b];
-    constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
-    const uint32_t sb0 = saddr(sB);
-    uint32_t lph = 0, ph1 = 0, ph2 = 0;  // tile-load phases (bit b); A-slot barrier phases
-    // Warp 0 waits until the MMAs that read A slot `slot` last have completed; the CTA barrier that
-    // follows every call releases the other warps.
-    auto slot_wait = [&](int slot) {
-        uint32_t& ph = slot ? ph2 : ph1;
-        if (warp == 0 && !s_abort && !mbar_wait_bounded(&bars[1 + slot], ph & 1u) && lane == 0) s_abort = 1;
-        ph++;
-    };
-    auto issue_mma = [&](int s) {  // slice s against every B slice t with s + t <= 6
-        const uint32_t aslot = tmem + kOzASlot + 32u * uint32_t(s & 1);
+                    for (int t = 0; t < kOzSlices; t++) {
+                        if (s + t >= kOzSlices) break;
+                        const uint32_t acc = tmem + 64u * uint32_t(min(s + t, kOzAcc - 1));
+                        const uint32_t bs = sb0 + uint32_t(t) * kOzSliceBytes;
 #pragma unroll
-        for (int t = 0; t < kOzSlices; t++) {
-            if (s + t >= kOzSlices) break;
-            const uint32_t acc = tmem + 64u * uint32_t(min(s + t, kOzAcc - 1));
-            const uint32_t bs = sb0 + uint32_t(t) * kOzSliceBytes;
-#pragma unroll
-            for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
-                tc_mma_f16_ta(acc, aslot + 8u * ks, tc_smem_desc(bs + 256u * ks, 128u, 1024u), idesc,
-                              (s > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
-        }
-        tc_commit(&bars[1 + (s & 1)]);
-    };
-    double rare_out[2 * kOzRows];
-
-    for (uint64_t it = 0; it < nmy; it++) {
-        const int b = int(it & 1);
-        if (it + 1 < nmy) issue_load(it + 1, b ^ 1);  // that buffer's tile was written back last iteration
-        if (warp == 0 && !mbar_wait_bounded(&bars[3 + b], (lph >> b) & 1u) && lane == 0) s_abort = 1;
-        lph ^= 1u << b;
-        __syncthreads();  // releases the warps that did not poll
-        if (s_abort) break;
-        double2* tl = tiles + size_t(b) * tsize;
-
-        // this thread's 8 amplitudes, the column's exponent
-        long long X[2 * kOzRows];
-        uint32_t emax = 0;
-        {
-            double2 v[kOzRows];
-            uint32_t r = col0;
-#pragma unroll
-            for (int i = 0; i < kOzRows; i++) {
-                if (i > 0) r ^= w[low_bit(i)];
-                v[gray_code(i)] = tl[r];
+                        for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
+                            tc_mma_f16_ta(acc, aslot + 8u * ks, tc_smem_desc(bs + 256u * ks, 128u, 1024u), idesc,
+                                          (s > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
+                    }
+                    tc_commit(&bars[kBarFree + slot]);
+                    if (s == kOzSlices - 1) tc_commit(&bars[kBarAccFull]);
+                }
             }
-#pragma unroll
-            for (int j = 0; j < kOzRows; j++) emax = max(emax, max(fx_efield(v[j].x), fx_efield(v[j].y)));
-            ex[g * 128 + m] = emax;
-            __syncthreads();
-            emax = max(max(ex[m], ex[128 + m]), max(ex[256 + m], ex[384 + m]));
-            const uint32_t EE = max(emax, 1u);
-            const bool fin = emax != 0x7ffu;
-#pragma unroll
-            for (int j = 0; j < kOzRows; j++) {
-                X[2 * j] = (fin ? oz_encode(v[j].x, EE) : 0ll) + kOzBias;
-                X[2 * j + 1] = (fin ? oz_encode(v[j].y, EE) : 0ll) + kOzBias;
-            }
+            tc_commit(&bars[kBarDone]);  // arrives once every MMA issued above has completed
+            if (!mbar_wait_bounded(&bars[kBarDone], 0)) ok = false;
+            if (!ok) s_abort = 1;
         }
-        const bool rare = emax == 0x7ffu;
-
-        // slices 0..6 through the two A slots
+        __syncwarp();
+    } else {
+        // ---- the math warps
+        bool bad = s_abort != 0;
+        const int q = warp & 3, g = warp >> 2, m = 32 * q + lane;  // row group g: block rows 8 g .. 8 g + 7
+        const uint32_t quarter = uint32_t(32 * q) << 16;
+        const uint32_t col0 = tab[m] ^ ((g & 1) ? tab[131] : 0u) ^ ((g & 2) ? tab[132] : 0u);  // row 8 g
+        const uint32_t lrow0 = swz16(col0);  // the swizzle is its own inverse
+        uint32_t w[3], ub[3];
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            w[b] = tab[128 + b];
+            ub[b] = tab[136 + b];
+        }
         const uint32_t ta = tmem + quarter + kOzASlot + uint32_t(kOzRows * g);
-        auto put = [&](int s, const uint32_t (&pk)[kOzRows]) {
-            if (s >= 2) {
-                slot_wait(s & 1);
-                __syncthreads();
-            }
+        // The pieces of this thread, tid + 512 k, share unit bits 3..7, so their swizzle is one XOR.
+        const uint32_t swz = swz16(uint32_t(tid)) ^ uint32_t(tid);
+        auto issue_load = [&](uint64_t i, int b) {
+            const uint64_t tb = expand_index(first + i * stride, sa.outer);
+            double2* dst = tiles + size_t(b) * tsize;
+            for (uint32_t c = uint32_t(tid); c < tsize; c += kOzMath)
+                cp_async16(dst + (c ^ swz), state + tb + rowoff[c >> sa.RL] + (c & rmask));
+            cp_async_mbar_arrive(&bars[kBarLoad + b]);
+        };
+        // slice s of tile `it` into slot (7 it + s) % 4, once the MMAs that read that slot last are done
+        auto put = [&](uint64_t it, int s, const uint32_t(&pk)[kOzRows]) {
+            const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
+            const uint32_t slot = uint32_t(u & 3u);
+            if (u >= uint64_t(kOzSlots) && !bad &&
+                !mbar_wait_bounded(&bars[kBarFree + slot], uint32_t(((u >> 2) - 1u) & 1u)))
+                bad = true;
+            __syncwarp();
             tc_fence_after();
-            tc_st8u_nowait(ta + 32u * uint32_t(s & 1), pk);
+            tc_st8u_nowait(ta + 32u * slot, pk);
             tc_wait_st();
             tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0 && !s_abort) issue_mma(s);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bars[kBarFull + slot]);
         };
-        {
+        // R = the previous tile's outputs as integers (row 8 g + i: R[2 i] real, R[2 i + 1] imaginary)
+        long long R[2 * kOzRows];
+        auto drain = [&](uint64_t itp) {
+            if (!bad && !mbar_wait_bounded(&bars[kBarAccFull], uint32_t(itp & 1u))) bad = true;
+            __syncwarp();
+            tc_fence_after();
+#pragma unroll
+            for (int i = 0; i < kOzRows; i++) {  // one row (two D columns) at a time
+                uint32_t a[kOzAcc][2];
+#pragma unroll
+                for (int L = 0; L < kOzAcc; L++)
+                    tc_ld2_nowait(tmem + quarter + 64u * L + uint32_t(2 * kOzRows * g) + 2u * i, a[L]);
+                tc_wait_ld();
+#pragma unroll
+                for (int e = 0; e < 2; e++)
+                    R[2 * i + e] = oz_combine(__uint_as_float(a[0][e]), __uint_as_float(a[1][e]),
+                                              __uint_as_float(a[2][e]), __uint_as_float(a[3][e]),
+                                              __uint_as_float(a[4][e]), __uint_as_float(a[5][e]));
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bars[kBarAccFree]);
+        };
+        // the previous tile's outputs: rounded once, scaled, stored in place
+        auto finish = [&](uint64_t base, int kE, bool rare) {
+            if (rare) return;  // the FP64 path has stored this column
+            double2* dst = state + base;
+            uint32_t l = lrow0;
+#pragma unroll
+            for (int i = 0; i < kOzRows; i++) {
+                if (i > 0) l ^= ub[low_bit(i)];
+                const int r = gray_code(i);
+                double2 y;
+                y.x = oz_to_double(R[2 * r], kE + sscale[2 * kOzRows * g + 2 * r]);
+                y.y = oz_to_double(R[2 * r + 1], kE + sscale[2 * kOzRows * g + 2 * r + 1]);
+                dst[rowoff[l >> sa.RL] + (l & rmask)] = y;
+            }
+        };
+
+        if (nmy > 0 && !bad) issue_load(0, 0);
+        uint64_t base_prev = 0;
+        int kE_prev = 1;
+        bool rare_prev = false, left = false;
+        for (uint64_t it = 0; it < nmy; it++) {
+            const int b = int(it & 1u);
+            if (!bad && !mbar_wait_bounded(&bars[kBarLoad + b], uint32_t((it >> 1) & 1u))) bad = true;
+            const double2* tl = tiles + size_t(b) * tsize;
+
+            // the column's exponent over this thread's 8 amplitudes (read again to encode them below)
+            uint32_t emax = 0;
+            {
+                uint32_t r = col0;
+#pragma unroll
+                for (int i = 0; i < kOzRows; i++) {
+                    if (i > 0) r ^= w[low_bit(i)];
+                    const double2 v = tl[r];
+                    emax = max(emax, max(fx_efield(v.x), fx_efield(v.y)));
+                }
+            }
+            uint32_t* exb = ex + uint32_t(it & 1u) * kOzMath;
+            exb[g * 128 + m] = emax;
+            // Every math thread has read its amplitudes of tile it - 1 (and its FP64 columns) before
+            // this barrier, so that buffer takes the next load; a wait that gave up ends the loop here.
+            if (math_sync_or(bad)) {
+                left = true;
+                break;
+            }
+            if (it + 1 < nmy) issue_load(it + 1, b ^ 1);
+            emax = max(max(exb[m], exb[128 + m]), max(exb[256 + m], exb[384 + m]));
+            const uint64_t base = expand_index(first + it * stride, sa.outer);
+            const bool rare = emax == 0x7ffu;
+            if (rare) oz_rare_column(tl, tab, m, g, bd, state + base, rowoff, rmask, sa.RL, lrow0);
+
+            long long X[2 * kOzRows];
+            {
+                const uint32_t EE = max(emax, 1u);
+                uint32_t r = col0;
+#pragma unroll
+                for (int i = 0; i < kOzRows; i++) {
+                    if (i > 0) r ^= w[low_bit(i)];
+                    const double2 v = tl[r];
+                    const int j = gray_code(i);
+                    X[2 * j] = (rare ? 0ll : oz_encode(v.x, EE)) + kOzBias;
+                    X[2 * j + 1] = (rare ? 0ll : oz_encode(v.y, EE)) + kOzBias;
+                }
+            }
             uint32_t pk[kOzRows];
             oz_slice<0>(X, pk);
-            put(0, pk);
+            put(it, 0, pk);
             oz_slice<1>(X, pk);
-            put(1, pk);
+            put(it, 1, pk);
             oz_slice<2>(X, pk);
-            put(2, pk);
+            put(it, 2, pk);
             oz_slice<3>(X, pk);
-            put(3, pk);
-            oz_slice<4>(X, pk);
-            put(4, pk);
-            oz_slice<5>(X, pk);
-            put(5, pk);
-            oz_slice<6>(X, pk);
-            put(6, pk);
-        }
-        // columns with a non-finite amplitude: FP64 results from the tile, which no thread has written yet
-        if (rare) oz_rare_column(tl, tab, m, g, bd, rare_out);
-        slot_wait(1);  // slice 5
-        slot_wait(0);  // slice 6: every MMA of the tile has completed
-        if (__syncthreads_or(s_abort)) break;  // a wait gave up: leave the tile unwritten
-        tc_fence_after();
-
-        // R -> double for the thread's 8 rows (D columns 16 g .. + 15: row 8 g + i, real then imaginary)
-        const int kE = int(max(emax, 1u));
-#pragma unroll
-        for (int r2 = 0; r2 < kOzRows / 2; r2++) {  // two rows (four D columns) at a time
-            uint32_t a[kOzAcc][4];
-#pragma unroll
-            for (int L = 0; L < kOzAcc; L++)
-                tc_ld4_nowait(tmem + quarter + 64u * L + uint32_t(2 * kOzRows * g) + 4u * r2, a[L]);
-            tc_wait_ld();
-#pragma unroll
-            for (int e = 0; e < 4; e += 2) {
-                const int i = 2 * r2 + e / 2;  // row 8 g + i
-                double2 y;
-                if (!rare) {
-                    const int n0 = 2 * kOzRows * g + 4 * r2 + e;
-                    const long long R0 = oz_combine(__uint_as_float(a[0][e]), __uint_as_float(a[1][e]),
-                                                    __uint_as_float(a[2][e]), __uint_as_float(a[3][e]),
-                                                    __uint_as_float(a[4][e]), __uint_as_float(a[5][e]));
-                    const long long R1 = oz_combine(__uint_as_float(a[0][e + 1]), __uint_as_float(a[1][e + 1]),
-                                                    __uint_as_float(a[2][e + 1]), __uint_as_float(a[3][e + 1]),
-                                                    __uint_as_float(a[4][e + 1]), __uint_as_float(a[5][e + 1]));
-                    y.x = oz_to_double(R0, kE + sscale[n0]);
-                    y.y = oz_to_double(R1, kE + sscale[n0 + 1]);
-                } else {
-                    y.x = rare_out[2 * i];
-                    y.y = rare_out[2 * i + 1];
-                }
-                tl[oz_row(col0, tab, i)] = y;  // row 8 g + i: bits of i over tab[128..130]
+            put(it, 3, pk);
+            if (it > 0) {
+                drain(it - 1);  // frees the accumulators for this tile's MMAs
+                finish(base_prev, kE_prev, rare_prev);  // overlaps this tile's first MMAs
             }
+            oz_slice<4>(X, pk);
+            put(it, 4, pk);
+            oz_slice<5>(X, pk);
+            put(it, 5, pk);
+            oz_slice<6>(X, pk);
+            put(it, 6, pk);
+            base_prev = base;
+            kE_prev = int(max(emax, 1u));
+            rare_prev = rare;
         }
-        tc_fence_before();
-        __syncthreads();  // the tile is complete; the accumulators are free for the next tile
-        tc_fence_after();
-        const uint64_t base = expand_index(first + it * stride, sa.outer);
-        for (uint32_t c = uint32_t(tid); c < tsize; c += kOzThreads)
-            state[base + rowoff[c >> sa.RL] + (c & rmask)] = tl[c ^ swz];
-        __syncthreads();  // the buffer is free for the load two tiles ahead
+        if (!left && nmy > 0) {
+            drain(nmy - 1);
+            if (!bad) finish(base_prev, kE_prev, rare_prev);
+        }
+        cp_async_wait_all();  // copies of tiles the loop did not reach
+        if (bad) s_abort = 1;
     }
-    cp_async_wait_all();  // copies of tiles the loop did not reach
-    if (tid == 0 && s_abort) atomicExch(err, 1);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tc_dealloc(tmem, kOzTmemCols);
+    if (tid == 0 && s_abort) atomicExch(err, 1);
+    if (warp == kOzMathWarps) tc_dealloc(tmem, kOzTmemCols);
 }
 
 }  // namespace
@@ -378,7 +466,7 @@ cudaError_t launch_tile_oz(void* state, int n, const TileStage& st, int op_begin
     const StageArgs sa = stage_args(st, op_begin, op_end);
     const size_t tile_bytes = sizeof(double2) << st.T;
     const size_t smem = kOzBBytes + kOzScaleBytes + 2 * tile_bytes + 4 * size_t(kOzIdxWords) + sizeof(TileOp) +
-                        (sizeof(uint64_t) << sa.RH) + 512 * 4 + 5 * sizeof(uint64_t) + 16;
+                        (sizeof(uint64_t) << sa.RH) + 2 * kOzMath * 4 + kOzBars * sizeof(uint64_t) + 16;
     const uint64_t ntiles = 1ull << (n - st.T);
     int per_sm = 0;
     cudaError_t oe = resident_blocks(reinterpret_cast<const void*>(k_tile_oz), kOzThreads, smem, &per_sm);
