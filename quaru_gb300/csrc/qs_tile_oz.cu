@@ -76,18 +76,19 @@ constexpr long long kOzBias = 0x808080808080LL;  // X + bias: digits 1..6 are by
 constexpr float kMagic = 12582912.0f;            // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
-// X = round(|v| 2^(1077 - EE)) with the sign of v, for EE = max(largest exponent field of the
-// column, 1) >= v's exponent field: the significand with its implicit bit, shifted left by 2 and
-// right by EE - e with rounding to nearest (ties away from zero). |X| < 2^55.
-__device__ __forceinline__ long long oz_encode(double v, uint32_t EE) {
+// Xb = X + kOzBias for X = round(|v| 2^(1077 - EE)) with the sign of v, for EE = max(largest
+// exponent field of the column, 1) >= v's exponent field: the significand with its implicit bit,
+// shifted left by 2 and right by EE - e with rounding to nearest (ties away from zero); |X| < 2^55.
+// The sign and the bias go in together: X + bias = (|X| ^ sg) + (bias - sg) for sg = 0 or -1.
+__device__ __forceinline__ long long oz_encode_biased(double v, uint32_t EE) {
     const uint32_t hi = uint32_t(__double2hiint(v)), lo = uint32_t(__double2loint(v));
     const uint32_t e = (hi >> 20) & 0x7ffu;
     const uint32_t d = min(EE - max(e, 1u), 63u);
     // 2m = significand << 3 (< 2^56); X = ((2m >> d) + 1) >> 1 rounds m / 2^d to nearest
-    const uint64_t m2 = ((uint64_t((hi & 0xfffffu) | (e != 0u ? 0x100000u : 0u)) << 32) | lo) << 3;
+    const uint64_t m2 = ((uint64_t((hi & 0xfffffu) | (min(e, 1u) << 20)) << 32) | lo) << 3;
     const uint64_t X = ((m2 >> d) + 1u) >> 1;
     const long long sg = (long long)(int32_t(hi) >> 31);  // 0 or -1
-    return ((long long)X ^ sg) - sg;
+    return ((long long)X ^ sg) + (kOzBias - sg);
 }
 
 // Digit s of Xb = X + kOzBias as a float, scaled by 2^-8s (s = 0: the signed top part Xb >> 48;
@@ -116,21 +117,59 @@ __device__ __forceinline__ void oz_slice(const long long (&X)[2 * kOzRows], uint
         pk[c] = __byte_perm(oz_digit_bits<S>(X[2 * c]), oz_digit_bits<S>(X[2 * c + 1]), 0x7632u);
 }
 
+// a * b + c with a 64-bit addend and result (one wide multiply-add).
+__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
+    long long d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+}
+
 // R = 2^36 (acc_0 + ... + acc_5) as an integer: levels 0..3 through the magic-number conversion
-// (|I_L| < 2^22), level 4 by a rounding conversion (|I_4| < 2^23), the tail rounded at 2^-36.
+// (|I_L| < 2^22: i_L = bits(acc_L 2^8L + 1.5 2^23) - bits(1.5 2^23)), level 4 by a rounding
+// conversion (|I_4| < 2^23), the tail rounded at 2^-36;
+// R = (i0 256 + i1) 2^28 + (i2 256 + i3) 2^12 + i4 2^4 + t, the magic constants folded into one
+// subtraction per partial sum (arithmetic modulo 2^32; the sums fit in 31 bits).
 __device__ __forceinline__ long long oz_combine(float a0, float a1, float a2, float a3, float a4, float a5) {
-    const int i0 = __float_as_int(a0 + kMagic) - kMagicBits;
-    const int i1 = __float_as_int(fmaf(a1, 256.0f, kMagic)) - kMagicBits;
-    const int i2 = __float_as_int(fmaf(a2, 65536.0f, kMagic)) - kMagicBits;
-    const int i3 = __float_as_int(fmaf(a3, 16777216.0f, kMagic)) - kMagicBits;
+    const uint32_t b0 = __float_as_uint(a0 + kMagic);
+    const uint32_t b1 = __float_as_uint(fmaf(a1, 256.0f, kMagic));
+    const uint32_t b2 = __float_as_uint(fmaf(a2, 65536.0f, kMagic));
+    const uint32_t b3 = __float_as_uint(fmaf(a3, 16777216.0f, kMagic));
     const int i4 = __float2int_rn(a4 * 4294967296.0f);
-    const int t = __float_as_int(fmaf(a5, 68719476736.0f, kMagic)) - kMagicBits;
-    const int j01 = i0 * 256 + i1, j23 = i2 * 256 + i3;  // below 2^28 and 2^30
-    return ((long long)j01 << 28) + ((long long)j23 << 12) + ((long long)i4 << 4) + (long long)t;
+    const uint32_t bt = __float_as_uint(fmaf(a5, 68719476736.0f, kMagic));
+    constexpr uint32_t kM257 = 257u * uint32_t(kMagicBits);
+    const int j01 = int(b0 * 256u + b1 - kM257);  // i0 256 + i1, |j01| < 2^30 + 2^22
+    const int j23 = int(b2 * 256u + b3 - kM257);  // i2 256 + i3
+    const int low = int(uint32_t(i4) * 16u + bt - uint32_t(kMagicBits));  // i4 16 + t, |low| < 2^28
+    return mad_wide(j01, 1 << 28, mad_wide(j23, 1 << 12, (long long)low));
 }
 
 __device__ __forceinline__ double oz_to_double(long long R, int k) {
     return (k >= kFxFastKMin && k <= kFxFastKMax) ? fx_to_double_fast(R, k << 20) : fx_to_double_any(R, k);
+}
+
+// R 2^k for kk = k << 20, k in [kFxFastKMin, kFxFastKMax] (the exponent field stays normal): a
+// non-zero integer converts to |d| >= 1, so a zero high word means R = 0 (and the result +0).
+__device__ __forceinline__ double oz_scale_fast(long long R, int kk) {
+    const double d = __ll2double_rn(R);
+    const int h = __double2hiint(d);
+    return __hiloint2double(h != 0 ? h + kk : 0, __double2loint(d));
+}
+
+// Wait for the phase of `parity`, suspending between polls (the hint bounds each suspension; the
+// thread resumes when the phase completes), at most `limit` SM clocks; false if the wait gave up.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, long long limit = 4000000000LL) {
+    const uint32_t a = saddr(bar);
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity), "r"(10000000u)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > limit) return false;
+    }
 }
 
 // Amplitude offset (16-byte units, swizzled) of block row j of this thread's column.
@@ -201,6 +240,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     uint64_t* bars = reinterpret_cast<uint64_t*>(ex + 2 * kOzMath);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + kOzBars);
     __shared__ int s_abort;
+    __shared__ int s_srange[2];  // smallest and largest output exponent
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ops + sa.op_begin);
         uint32_t* dst = reinterpret_cast<uint32_t*>(sop);
@@ -251,6 +291,16 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     }
     if (warp == 0 && !mbar_wait_bounded(&bars[kBarB], 0) && lane == 0) s_abort = 1;
     __syncthreads();
+    if (tid == 0) {
+        int lo = sscale[0], hi = sscale[0];
+        for (int n = 1; n < 64; n++) {
+            lo = min(lo, sscale[n]);
+            hi = max(hi, sscale[n]);
+        }
+        s_srange[0] = lo;
+        s_srange[1] = hi;
+    }
+    __syncthreads();
     const double* bd = reinterpret_cast<const double*>(bfrag + kOzBBytes + kOzScaleBytes);
 
     const uint64_t first = blockIdx.x, stride = gridDim.x;
@@ -267,12 +317,12 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 for (int s = 0; s < kOzSlices; s++) {
                     const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
                     const uint32_t slot = uint32_t(u & 3u);
-                    if (!mbar_wait_bounded(&bars[kBarFull + slot], uint32_t((u >> 2) & 1u))) {
+                    if (!mbar_wait_sleep(&bars[kBarFull + slot], uint32_t((u >> 2) & 1u))) {
                         ok = false;
                         break;
                     }
                     // a tile's first MMAs overwrite the accumulators: the previous tile's must be drained
-                    if (s == 0 && it > 0 && !mbar_wait_bounded(&bars[kBarAccFree], uint32_t((it - 1) & 1u))) {
+                    if (s == 0 && it > 0 && !mbar_wait_sleep(&bars[kBarAccFree], uint32_t((it - 1) & 1u))) {
                         ok = false;
                         break;
                     }
@@ -293,7 +343,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 }
             }
             tc_commit(&bars[kBarDone]);  // arrives once every MMA issued above has completed
-            if (!mbar_wait_bounded(&bars[kBarDone], 0)) ok = false;
+            if (!mbar_wait_sleep(&bars[kBarDone], 0)) ok = false;
             if (!ok) s_abort = 1;
         }
         __syncwarp();
@@ -313,19 +363,23 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         const uint32_t ta = tmem + quarter + kOzASlot + uint32_t(kOzRows * g);
         // The pieces of this thread, tid + 512 k, share unit bits 3..7, so their swizzle is one XOR.
         const uint32_t swz = swz16(uint32_t(tid)) ^ uint32_t(tid);
-        auto issue_load = [&](uint64_t i, int b) {
+        // load tile i into buffer b; returns the tile's base amplitude index
+        auto issue_load = [&](uint64_t i, int b) -> uint64_t {
             const uint64_t tb = expand_index(first + i * stride, sa.outer);
             double2* dst = tiles + size_t(b) * tsize;
+            const double2* src = state + tb;
             for (uint32_t c = uint32_t(tid); c < tsize; c += kOzMath)
-                cp_async16(dst + (c ^ swz), state + tb + rowoff[c >> sa.RL] + (c & rmask));
+                cp_async16(dst + (c ^ swz), src + rowoff[c >> sa.RL] + (c & rmask));
             cp_async_mbar_arrive(&bars[kBarLoad + b]);
+            return tb;
         };
+
         // slice s of tile `it` into slot (7 it + s) % 4, once the MMAs that read that slot last are done
         auto put = [&](uint64_t it, int s, const uint32_t(&pk)[kOzRows]) {
             const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
             const uint32_t slot = uint32_t(u & 3u);
             if (u >= uint64_t(kOzSlots) && !bad &&
-                !mbar_wait_bounded(&bars[kBarFree + slot], uint32_t(((u >> 2) - 1u) & 1u)))
+                !mbar_wait_sleep(&bars[kBarFree + slot], uint32_t(((u >> 2) - 1u) & 1u)))
                 bad = true;
             __syncwarp();
             tc_fence_after();
@@ -338,7 +392,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         // R = the previous tile's outputs as integers (row 8 g + i: R[2 i] real, R[2 i + 1] imaginary)
         long long R[2 * kOzRows];
         auto drain = [&](uint64_t itp) {
-            if (!bad && !mbar_wait_bounded(&bars[kBarAccFull], uint32_t(itp & 1u))) bad = true;
+            if (!bad && !mbar_wait_sleep(&bars[kBarAccFull], uint32_t(itp & 1u))) bad = true;
             __syncwarp();
             tc_fence_after();
 #pragma unroll
@@ -362,25 +416,33 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         auto finish = [&](uint64_t base, int kE, bool rare) {
             if (rare) return;  // the FP64 path has stored this column
             double2* dst = state + base;
+            const int* ss = sscale + 2 * kOzRows * g;
+            // a column exponent that keeps every output exponent in the fast conversion range
+            const bool fast = kE + s_srange[0] >= kFxFastKMin && kE + s_srange[1] <= kFxFastKMax;
             uint32_t l = lrow0;
 #pragma unroll
             for (int i = 0; i < kOzRows; i++) {
                 if (i > 0) l ^= ub[low_bit(i)];
                 const int r = gray_code(i);
                 double2 y;
-                y.x = oz_to_double(R[2 * r], kE + sscale[2 * kOzRows * g + 2 * r]);
-                y.y = oz_to_double(R[2 * r + 1], kE + sscale[2 * kOzRows * g + 2 * r + 1]);
+                if (fast) {
+                    y.x = oz_scale_fast(R[2 * r], (kE + ss[2 * r]) << 20);
+                    y.y = oz_scale_fast(R[2 * r + 1], (kE + ss[2 * r + 1]) << 20);
+                } else {
+                    y.x = oz_to_double(R[2 * r], kE + ss[2 * r]);
+                    y.y = oz_to_double(R[2 * r + 1], kE + ss[2 * r + 1]);
+                }
                 dst[rowoff[l >> sa.RL] + (l & rmask)] = y;
             }
         };
 
-        if (nmy > 0 && !bad) issue_load(0, 0);
+        uint64_t base_next = (nmy > 0 && !bad) ? issue_load(0, 0) : 0;
         uint64_t base_prev = 0;
         int kE_prev = 1;
         bool rare_prev = false, left = false;
         for (uint64_t it = 0; it < nmy; it++) {
             const int b = int(it & 1u);
-            if (!bad && !mbar_wait_bounded(&bars[kBarLoad + b], uint32_t((it >> 1) & 1u))) bad = true;
+            if (!bad && !mbar_wait_sleep(&bars[kBarLoad + b], uint32_t((it >> 1) & 1u))) bad = true;
             const double2* tl = tiles + size_t(b) * tsize;
 
             // the column's exponent over this thread's 8 amplitudes (read again to encode them below)
@@ -402,9 +464,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                 left = true;
                 break;
             }
-            if (it + 1 < nmy) issue_load(it + 1, b ^ 1);
+            const uint64_t base = base_next;
+            if (it + 1 < nmy) base_next = issue_load(it + 1, b ^ 1);
             emax = max(max(exb[m], exb[128 + m]), max(exb[256 + m], exb[384 + m]));
-            const uint64_t base = expand_index(first + it * stride, sa.outer);
             const bool rare = emax == 0x7ffu;
             if (rare) oz_rare_column(tl, tab, m, g, bd, state + base, rowoff, rmask, sa.RL, lrow0);
 
@@ -417,8 +479,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     if (i > 0) r ^= w[low_bit(i)];
                     const double2 v = tl[r];
                     const int j = gray_code(i);
-                    X[2 * j] = (rare ? 0ll : oz_encode(v.x, EE)) + kOzBias;
-                    X[2 * j + 1] = (rare ? 0ll : oz_encode(v.y, EE)) + kOzBias;
+                    X[2 * j] = rare ? kOzBias : oz_encode_biased(v.x, EE);
+                    X[2 * j + 1] = rare ? kOzBias : oz_encode_biased(v.y, EE);
                 }
             }
             uint32_t pk[kOzRows];
@@ -446,7 +508,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         }
         if (!left && nmy > 0) {
             drain(nmy - 1);
-            if (!bad) finish(base_prev, kE_prev, rare_prev);
+            finish(base_prev, kE_prev, rare_prev);
         }
         cp_async_wait_all();  // copies of tiles the loop did not reach
         if (bad) s_abort = 1;
