@@ -399,6 +399,26 @@ def run_ours(args) -> None:
             fused["blocks"] = {"gates_per_s": len(fl) / bs, "ms_per_step": 1e3 * bs / args.steps,
                                "speedup_vs_unfused": dev_s / bs, "launches": int(lib.qs_launch_count() - l0),
                                "max_width": q.circuit_autotune(n, prec, arith, 2)["max_width"]}
+            # the same layers as FP64-accurate 5-qubit blocks: split-integer products on the BF16 tensor
+            # cores (k_tile_oz), one stage per block; time per stage from CUDA events around each launch
+            reg.set_arith(q.QS_ARITH_FX64)
+            reg.apply_gates([g for i in range(args.warmup) for g in layer(i)], fuse=2, max_width=5)
+            barrier()
+            o0 = torch.cuda.Event(enable_timing=True)
+            o1 = torch.cuda.Event(enable_timing=True)
+            l0 = lib.qs_launch_count()
+            o0.record(stream)
+            reg.apply_gates(fl, fuse=2, max_width=5)
+            o1.record(stream)
+            barrier()
+            os_ = o0.elapsed_time(o1) / 1e3
+            stages = int(lib.qs_launch_count() - l0)
+            reg.set_arith(arith)
+            fused["blocks_fx64_tensor"] = {
+                "gates_per_s": len(fl) / os_, "ms_per_step": 1e3 * os_ / args.steps, "speedup_vs_unfused": dev_s / os_,
+                "launches": stages, "ms_per_stage": 1e3 * os_ / stages,
+                "hbm_frac_per_stage": 2.0 * (1 << n) * 16 / (os_ / stages) / 1e9 / read_peaks()[0],
+                "arith": "FP64-accurate split-integer products on the BF16 tensor cores (tcgen05 kind::f16)"}
         if prec == q.QS_PREC_C64:
             # dense 5-qubit blocks as 3xTF32 tensor-core GEMMs
             b0 = torch.cuda.Event(enable_timing=True)
@@ -574,25 +594,33 @@ def measure_section(q, torch, args) -> dict:
 
 
 def width_section(q, torch, args) -> dict:
-    """The plain form at scale: a 28-qubit complex128 layered circuit (Haar on every qubit + a CNOT
+    """The plain form at scale (C2): a 28-qubit complex128 layered circuit (Haar on every qubit + a CNOT
     matching per layer) with fusion off (one sweep per gate), cache-blocked stages, and dense fused
-    blocks of width 2..5 (each block one sweep). Per variant: ms, gates/s, sweeps, and the HBM GB/s
-    those sweeps move (each gate's own bytes unfused, 2 * 2^n * 16 bytes per fused sweep).
-    Double-float arithmetic; blocks of 4 and 5 qubits run in FP64 (the double-float kernel covers up
-    to 3). Layers: 40 for the per-gate, stage and 2- and 3-qubit block runs, 10 for the FP64 4- and
-    5-qubit blocks."""
+    blocks of width 2..5 (each block one sweep or one tensor-core stage). Per variant: ms, gates/s,
+    sweeps, and the HBM GB/s those sweeps move (each gate's own bytes unfused, 2 * 2^n * 16 bytes per
+    fused sweep). Arithmetic per variant: plain FP64 (fused multiply-add; its blocks are FP64 dense
+    sweeps), the FP64-accurate fixed-point form (`fx64`: single sweeps on the integer pipes, blocks as
+    split-integer products on the BF16 tensor cores; every width pads its blocks to 5 qubits), and
+    double-float (`df64`, narrower than FP64: 24 + 24 significand bits) for comparison. Layers: 40,
+    except 10 for the FP64 blocks of 3..5 qubits, whose FP64 dense sweeps are slow."""
     from quaru_gb300.workloads import flatten, layered_circuit, seed_for
 
     n = 28
     lib = q._lib.load()
     reg = q.Register.from_int(n, 0)
-    reg.set_arith(q.QS_ARITH_DF64)
     stream = torch.cuda.ExternalStream(reg.stream)
     sweep_bytes = 2.0 * (1 << n) * 16
-    out = {"workload": f"{n}-qubit layered random circuit, complex128, double-float arithmetic", "qubits": n}
-    variants = [("unfused", 0, 5, 40), ("stages", 1, 5, 40), ("blocks_w2", 2, 2, 40), ("blocks_w3", 2, 3, 40),
-                ("blocks_w4", 2, 4, 10), ("blocks_w5", 2, 5, 10)]
-    for name, fuse, width, layers in variants:
+    out = {"workload": f"{n}-qubit layered random circuit (per layer: Haar 1q on every qubit + {n // 2} CNOTs on "
+                       f"a random perfect matching), complex128", "qubits": n}
+    A = {"fma": q.QS_ARITH_FMA, "fx64": q.QS_ARITH_FX64, "df64": q.QS_ARITH_DF64}
+    variants = [("fma_unfused", "fma", 0, 5, 40), ("fma_stages", "fma", 1, 5, 40), ("fma_blocks_w2", "fma", 2, 2, 40),
+                ("fma_blocks_w3", "fma", 2, 3, 10), ("fma_blocks_w4", "fma", 2, 4, 10), ("fma_blocks_w5", "fma", 2, 5, 10),
+                ("fx64_unfused", "fx64", 0, 5, 40), ("fx64_blocks_w2", "fx64", 2, 2, 40),
+                ("fx64_blocks_w3", "fx64", 2, 3, 40), ("fx64_blocks_w4", "fx64", 2, 4, 40),
+                ("fx64_blocks_w5", "fx64", 2, 5, 40),
+                ("df64_unfused", "df64", 0, 5, 40), ("df64_blocks_w3", "df64", 2, 3, 40)]
+    for name, ar, fuse, width, layers in variants:
+        reg.set_arith(A[ar])
         ops = flatten(layered_circuit(n, layers, seed_for(2)))
         reg.apply_gates(ops[: 3 * (n + n // 2)], fuse=fuse, max_width=width)  # warm-up: 3 layers
         reg.synchronize()
@@ -607,8 +635,11 @@ def width_section(q, torch, args) -> dict:
         sweeps = int(lib.qs_launch_count() - l0)
         # bytes the sweeps move: per gate (a CNOT touches half the state) unfused, whole states otherwise
         moved = sum(gate_bytes(g, n, 16) for g in ops) if fuse == 0 else sweeps * sweep_bytes
-        out[name] = {"layers": layers, "gates": len(ops), "ms": 1e3 * s, "gates_per_s": len(ops) / s,
-                     "sweeps": sweeps, "hbm_gbs": moved / s / 1e9}
+        out[name] = {"arith": ar, "fuse": fuse, "max_width": width if fuse == 2 else None, "layers": layers,
+                     "gates": len(ops), "ms": 1e3 * s, "gates_per_s": len(ops) / s, "sweeps": sweeps,
+                     "hbm_gbs": moved / s / 1e9}
+    out["fx64_blocks_w5_vs_fma_unfused"] = out["fx64_blocks_w5"]["gates_per_s"] / out["fma_unfused"]["gates_per_s"]
+    out["fx64_blocks_w5_vs_fx64_unfused"] = out["fx64_blocks_w5"]["gates_per_s"] / out["fx64_unfused"]["gates_per_s"]
     return out
 
 
@@ -624,12 +655,17 @@ def precision_section(q, torch, args) -> dict:
     layers = layered_circuit(n, 40, seed_for(3))
     torch.cuda.synchronize()
     regs = {"fp64_plain": q.Register.from_int(n, 0),
+            "c128_fx64": q.Register.from_int(n, 0),
+            "c128_fx64_blocks": q.Register.from_int(n, 0),
             "c128_df64": q.Register.from_int(n, 0),
             "c64_passes": q.Register.from_int(n, 0, precision=q.QS_PREC_C64),
             "c64_blocks_tf32x3": q.Register.from_int(n, 0, precision=q.QS_PREC_C64)}
     regs["fp64_plain"].set_arith(q.QS_ARITH_FMA)  # the plain FP64 form: FP64 fused multiply-add
+    regs["c128_fx64"].set_arith(q.QS_ARITH_FX64)  # FP64-accurate fixed point, one sweep per gate
+    regs["c128_fx64_blocks"].set_arith(q.QS_ARITH_FX64)  # FP64-accurate 5-qubit blocks on the tensor cores
     regs["c128_df64"].set_arith(q.QS_ARITH_DF64)
-    fuse = {"fp64_plain": 0, "c128_df64": 0, "c64_passes": 1, "c64_blocks_tf32x3": 2}
+    fuse = {"fp64_plain": 0, "c128_fx64": 0, "c128_fx64_blocks": 2, "c128_df64": 0, "c64_passes": 1,
+            "c64_blocks_tf32x3": 2}
     secs = {k: 0.0 for k in regs}
     gates = 0
     checkpoints = []
@@ -648,7 +684,7 @@ def precision_section(q, torch, args) -> dict:
         ref = regs["fp64_plain"]
         nref = ref.inner_product(ref).real
         cp = {"layers": 10 * (k + 1)}
-        for name in ("c128_df64", "c64_passes", "c64_blocks_tf32x3"):
+        for name in ("c128_fx64", "c128_fx64_blocks", "c128_df64", "c64_passes", "c64_blocks_tf32x3"):
             r = regs[name]
             f = abs(r.inner_product(ref)) ** 2 / (nref * r.inner_product(r).real)
             cp[f"one_minus_fidelity_{name}"] = 1.0 - f
@@ -658,6 +694,7 @@ def precision_section(q, torch, args) -> dict:
            "gates_per_s": {k: gates / v for k, v in secs.items()}}
     out["mixed_vs_fp64_gates_per_s"] = {k: secs["fp64_plain"] / secs[k]
                                         for k in ("c128_df64", "c64_passes", "c64_blocks_tf32x3")}
+    out["fp64_accurate_vs_fp64_gates_per_s"] = {k: secs["fp64_plain"] / secs[k] for k in ("c128_fx64", "c128_fx64_blocks")}
     out["fp64_plain_arith"] = "FP64 fused multiply-add, one sweep per gate"
     del regs
     return out

@@ -55,7 +55,9 @@ extern "C" {
 #define QS_ARITH_FX64 3  /* FP64-accurate fixed-point arithmetic on the integer pipes for dense
                             1-qubit gates: each output is an exact-to-2^-55 integer dot product
                             rounded once to double (error <= ulp/2 + 2^-55 max|u| max|x|, below
-                            the FP64 FMA form's); other gates and fused stages use FP64 FMA */
+                            the FP64 FMA form's); fused dense blocks (qs_apply_circuit, fuse = 2,
+                            12 qubits and more) run as FP64-accurate split-integer products on the
+                            BF16 tensor cores; other gates and cache-blocked stages use FP64 FMA */
 
 typedef struct qs_register qs_register;
 
@@ -118,8 +120,9 @@ typedef struct qs_gate {
 typedef struct qs_circuit_options {
     int fuse;        /* 0: one sweep per gate; 1: cache-blocked stages (bit-identical to 0
                         under QS_ARITH_EXACT); 2: dense fused blocks (complex64 registers:
-                        3xTF32 tensor-core blocks); 3: the autotuner picks 0, 1 (and its tile
-                        size) or 2 (and its width) */
+                        3xTF32 tensor-core blocks; complex128 registers in QS_ARITH_FX64:
+                        FP64-accurate split-integer tensor-core blocks); 3: the autotuner picks
+                        0, 1 (and its tile size) or 2 (and its width) */
     int max_width;   /* widest fused dense block, 2..5 (fuse == 2); 0 = autotuned (see
                         qs_circuit_autotune) */
     int tile_qubits; /* qubits per shared-memory tile for fuse == 1; 0 = autotuned */
@@ -130,7 +133,7 @@ typedef struct qs_circuit_options {
  * passes by hand, src/operation.rs:114-269): the candidates of `fuse` (1: tile
  * sizes of stages; 2: block widths 2..5; 3: both, plus one sweep per gate) are
  * timed once per (n, precision, arith, fuse) on a scratch register running a
- * seeded stand-in workload of the benchmarks' family (two layers of random
+ * seeded stand-in workload of the benchmarks' family (six layers of random
  * dense 1-qubit gates on every qubit and CNOTs on a random matching) at
  * min(n, 26) qubits; the fastest is kept in memory and in the autotune cache
  * file (QS_AUTOTUNE_CACHE, default ~/.cache/quaru_gb300_autotune.txt). Later

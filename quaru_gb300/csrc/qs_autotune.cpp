@@ -7,7 +7,7 @@
 // number of blocks sharing a mid-size state. The reference's counterpart is a caller choosing
 // QuantumCircuit reduction passes by hand (src/operation.rs:114-269; the timings in
 // examples/circuit_example.rs:24-28). Here candidates are timed once per (size, precision,
-// arithmetic, mode) on a scratch register running a seeded stand-in workload (two layers of
+// arithmetic, mode) on a scratch register running a seeded stand-in workload (six layers of
 // Haar-random 1-qubit gates on every qubit and CNOTs on a random perfect matching, the
 // benchmarks' circuit family) at min(n, 26) qubits, and the fastest is cached.
 #include <cuda_runtime.h>
@@ -64,7 +64,7 @@ void autotune_cache_store(const std::string& key, int a, int b) {
 namespace {
 
 constexpr int kTuneMaxQubits = 26;
-constexpr int kTuneLayers = 2;
+constexpr int kTuneLayers = 6;  // enough layers that fusion across layer boundaries shows
 
 uint64_t splitmix(uint64_t* s) {
     uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
@@ -142,7 +142,7 @@ void make_workload(int n, Workload* w) {
 
 std::string tune_key(int n, int prec, int arith, int mode) {
     std::ostringstream k;
-    k << "circuit1:n" << n << ":p" << prec << ":a" << arith << ":m" << mode;
+    k << "circuit2:n" << n << ":p" << prec << ":a" << arith << ":m" << mode;
     return k.str();
 }
 
