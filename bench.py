@@ -794,8 +794,9 @@ def run_kernels(args) -> None:
     init (basis and product state), dense 1-qubit (exact, FMA, DF64, fixed point; complex64),
     CNOT/permutation, dense 3-qubit, 6-qubit permutation and dense gates, probability reduction,
     read-back and collapse (both precisions), measurement sequences (fused collapse + next sums;
-    reference-order sums), stages (complex128 DF64 tiles, complex64 register passes, complex64 3xTF32
-    tensor-core blocks), adjoint (FP64 and mixed), batch (FP64 and mixed)."""
+    reference-order sums), stages (complex128 FMA tiles, complex128 FP64-accurate tensor-core blocks,
+    complex64 register passes, complex64 3xTF32 tensor-core blocks), adjoint (FP64 and mixed), batch
+    (FP64 and mixed)."""
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
@@ -821,6 +822,7 @@ def run_kernels(args) -> None:
         small.apply_gates(layers[:12] if n == 12 else flatten(layered_circuit(12, 1, 7)))
         small.measure_sequence(list(range(12)), [0.5] * 12)
         r.apply_gates(layers, fuse=1)
+        r.apply_gates(layers, fuse=2, max_width=5)  # fixed point: FP64-accurate tensor-core blocks
         # wide gates (out-of-place kernels), a product-state register, the probability read-back
         perm = np.eye(64)[np.random.default_rng(2).permutation(64)]
         r.try_apply_fast(O.Operation(perm, [0, 3, 7, 11, n - 5, n - 2]))
