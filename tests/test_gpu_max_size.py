@@ -4,8 +4,10 @@ No CPU oracle can follow states of 32 and 33 qubits, so these tests check proper
 depend on the size: single-qubit marginals of basis states are exactly 0 or 1; H on the top qubit
 splits it evenly; measuring collapses the other qubits back to exact 0/1 marginals; a circuit
 followed by its inverse returns to the basis state it started from (fused forward, unfused or
-differently fused inverse, so the two paths check each other); a product state's marginals are
-|b_q|^2. Every amplitude index above bit 31 goes through the kernels' 64-bit index arithmetic.
+differently fused inverse, so the two paths check each other: register passes, 3xTF32 and
+FP64-accurate tensor-core blocks, FMA and double-float tiles, single sweeps); a product state's
+marginals are |b_q|^2. Every amplitude index above bit 31 goes through the kernels' 64-bit index
+arithmetic.
 Each test skips when the GPU has less free memory than its state needs.
 """
 from __future__ import annotations
@@ -113,6 +115,27 @@ def test_circuit_and_inverse_32_qubits_c128(q, arith):
     r = q.Register.from_int(n, k)
     r.set_arith(arith)
     r.apply_gates(ops, fuse=1)
+    m = marginals(q, r)
+    assert np.all((m > 1e-4) & (m < 1 - 1e-4))
+    r.apply_gates(inverse(ops), fuse=0)
+    norms: list = []
+    assert np.max(np.abs(marginals(q, r, norms) - bits_of(k, n))) < 1e-11
+    assert max(abs(x - 1.0) for x in norms) < 1e-12
+
+
+def test_fixed_point_blocks_and_inverse_32_qubits_c128(q):
+    """complex128, 32 qubits: the FP64-accurate tensor-core blocks (fixed-point arithmetic, fuse = 2:
+    one 5-qubit block per 12-qubit tile stage, tile indices past bit 19, amplitude indices past bit
+    31), inverse as fixed-point single sweeps; FP64-level agreement."""
+    from quaru_gb300.workloads import flatten, layered_circuit
+
+    n = 32
+    need_bytes(16 << n)
+    k = (1 << 31) | (1 << 29) | 0x4321
+    ops = flatten(layered_circuit(n, 2, 4300))
+    r = q.Register.from_int(n, k)
+    r.set_arith(q.QS_ARITH_FX64)
+    r.apply_gates(ops, fuse=2, max_width=5)
     m = marginals(q, r)
     assert np.all((m > 1e-4) & (m < 1 - 1e-4))
     r.apply_gates(inverse(ops), fuse=0)
