@@ -712,7 +712,7 @@ def adjoint_section(q, torch, args) -> dict:
     out = {"workload": "20-qubit hardware-efficient ansatz, 10 layers (RY, RZ on every qubit + CNOT ladder), "
                        "400 parameters, H = sum a_i Z_i Z_i+1 + sum b_i X_i"}
     grads = {}
-    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("fp64_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
+    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("c128_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
                               ("mixed", q.QS_PREC_C64, q.QS_ARITH_FMA)):
         reg = q.Register.from_int(n, 0, precision=prec)
         reg.set_arith(arith)
@@ -726,7 +726,7 @@ def adjoint_section(q, torch, args) -> dict:
         grads[name] = g
         out[name] = {"ms_per_gradient": 1e3 * dt, "grads_per_s": len(params) / dt, "energy": e}
     out["mixed_vs_fp64_speedup"] = out["fp64"]["ms_per_gradient"] / out["mixed"]["ms_per_gradient"]
-    out["max_grad_diff_df64_vs_fp64"] = float(np.max(np.abs(grads["fp64_df64"] - grads["fp64"])))
+    out["max_grad_diff_df64_vs_fp64"] = float(np.max(np.abs(grads["c128_df64"] - grads["fp64"])))
     out["max_grad_diff_mixed_vs_fp64"] = float(np.max(np.abs(grads["mixed"] - grads["fp64"])))
     a = q.Register.from_int(n, 0)
     a.set_arith(q.QS_ARITH_FMA)
@@ -750,7 +750,7 @@ def batch_section(q, args) -> dict:
     ngrads = len(params)
     out = {"workload": "256 ansatz circuits, qubits ~ U{10..22}, layers ~ U{4..12}, random Z/ZZ/X observables",
            "circuits": len(circuits), "parameters": ngrads}
-    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("fp64_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
+    for name, prec, arith in (("fp64", q.QS_PREC_C128, q.QS_ARITH_FMA), ("c128_df64", q.QS_PREC_C128, q.QS_ARITH_DF64),
                               ("mixed", q.QS_PREC_C64, q.QS_ARITH_FMA)):
         t0 = time.perf_counter()
         b = Batch(circuits, precision=prec, arith=arith)
