@@ -172,6 +172,36 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, 
     }
 }
 
+// The MMAs of A slice S (tensor-memory columns from aslot) against every B slice t with S + t <= 6
+// (descriptor of B slice 0: bdesc0; slice t and K step ks start (8192 t + 256 ks) bytes further, an
+// offset the descriptor's 14-bit start-address field absorbs without carry), into the level
+// accumulators; a tile's first slice starts levels 0..5 afresh. Unrolled per slice, so every
+// offset and accumulate flag is a constant.
+template <int S>
+__device__ __forceinline__ void oz_issue_slice(uint32_t tmem, uint32_t aslot, uint64_t bdesc0) {
+    constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
+#pragma unroll
+    for (int t = 0; t + S < kOzSlices; t++) {
+        const uint32_t acc = tmem + 64u * uint32_t(min(S + t, kOzAcc - 1));
+#pragma unroll
+        for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
+            tc_mma_f16_ta(acc, aslot + 8u * ks, bdesc0 + ((uint64_t(t) * kOzSliceBytes + 256u * ks) >> 4), idesc,
+                          (S > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
+    }
+}
+
+// Wait for the phase of `parity` with short sleeps between polls (the math warps: their polls would
+// otherwise take issue slots from the warps that share their scheduler), at most `limit` SM clocks;
+// false if the wait gave up.
+__device__ __forceinline__ bool mbar_wait_nap(uint64_t* bar, uint32_t parity, long long limit = 4000000000LL) {
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        __nanosleep(40);
+        if (clock64() - t0 > limit) return false;
+    }
+}
+
 // Amplitude offset (16-byte units, swizzled) of block row j of this thread's column.
 __device__ __forceinline__ uint32_t oz_row(uint32_t col0, const uint32_t* tab, int j) {
     uint32_t r = col0;
@@ -311,8 +341,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         // ---- the MMA warp: slice s of a tile against every B slice t with s + t <= 6
         if (lane == 0) {
             bool ok = s_abort == 0;
-            constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
-            const uint32_t sb0 = saddr(sB);
+            const uint64_t bdesc0 = tc_smem_desc(saddr(sB), 128u, 1024u);
             for (uint64_t it = 0; ok && it < nmy; it++) {
                 for (int s = 0; s < kOzSlices; s++) {
                     const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
@@ -328,15 +357,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     }
                     tc_fence_after();
                     const uint32_t aslot = tmem + kOzASlot + 32u * slot;
-#pragma unroll
-                    for (int t = 0; t < kOzSlices; t++) {
-                        if (s + t >= kOzSlices) break;
-                        const uint32_t acc = tmem + 64u * uint32_t(min(s + t, kOzAcc - 1));
-                        const uint32_t bs = sb0 + uint32_t(t) * kOzSliceBytes;
-#pragma unroll
-                        for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
-                            tc_mma_f16_ta(acc, aslot + 8u * ks, tc_smem_desc(bs + 256u * ks, 128u, 1024u), idesc,
-                                          (s > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
+                    switch (s) {
+                        case 0: oz_issue_slice<0>(tmem, aslot, bdesc0); break;
+                        case 1: oz_issue_slice<1>(tmem, aslot, bdesc0); break;
+                        case 2: oz_issue_slice<2>(tmem, aslot, bdesc0); break;
+                        case 3: oz_issue_slice<3>(tmem, aslot, bdesc0); break;
+                        case 4: oz_issue_slice<4>(tmem, aslot, bdesc0); break;
+                        case 5: oz_issue_slice<5>(tmem, aslot, bdesc0); break;
+                        default: oz_issue_slice<6>(tmem, aslot, bdesc0); break;
                     }
                     tc_commit(&bars[kBarFree + slot]);
                     if (s == kOzSlices - 1) tc_commit(&bars[kBarAccFull]);
@@ -379,7 +407,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
             const uint64_t u = uint64_t(kOzSlices) * it + uint64_t(s);
             const uint32_t slot = uint32_t(u & 3u);
             if (u >= uint64_t(kOzSlots) && !bad &&
-                !mbar_wait_sleep(&bars[kBarFree + slot], uint32_t(((u >> 2) - 1u) & 1u)))
+                !mbar_wait_nap(&bars[kBarFree + slot], uint32_t(((u >> 2) - 1u) & 1u)))
                 bad = true;
             __syncwarp();
             tc_fence_after();
@@ -392,7 +420,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         // R = the previous tile's outputs as integers (row 8 g + i: R[2 i] real, R[2 i + 1] imaginary)
         long long R[2 * kOzRows];
         auto drain = [&](uint64_t itp) {
-            if (!bad && !mbar_wait_sleep(&bars[kBarAccFull], uint32_t(itp & 1u))) bad = true;
+            if (!bad && !mbar_wait_nap(&bars[kBarAccFull], uint32_t(itp & 1u))) bad = true;
             __syncwarp();
             tc_fence_after();
 #pragma unroll
@@ -442,7 +470,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         bool rare_prev = false, left = false;
         for (uint64_t it = 0; it < nmy; it++) {
             const int b = int(it & 1u);
-            if (!bad && !mbar_wait_sleep(&bars[kBarLoad + b], uint32_t((it >> 1) & 1u))) bad = true;
+            if (!bad && !mbar_wait_nap(&bars[kBarLoad + b], uint32_t((it >> 1) & 1u))) bad = true;
             const double2* tl = tiles + size_t(b) * tsize;
 
             // the column's exponent over this thread's 8 amplitudes (read again to encode them below)
