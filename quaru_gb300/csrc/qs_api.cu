@@ -197,6 +197,10 @@ void touch_qubits(qs_register* reg, const double* matrix, const size_t* targets,
 // up to this size; larger registers and the other forms use the parallel tree reduction.
 constexpr int kSequentialMaxQubits = 20;
 
+// Registers in the reference's arithmetic divide by sqrt(total) with the correctly rounded quotient
+// (bit-identical collapses); the other forms multiply by its reciprocal (within one ulp).
+bool exact_quotient(const qs_register* reg) { return reg->prec == QS_PREC_C128 && reg->arith == QS_ARITH_EXACT; }
+
 bool sequential_sums(const qs_register* reg) {
     return reg->prec == QS_PREC_C128 && reg->arith == QS_ARITH_EXACT && reg->n <= kSequentialMaxQubits;
 }
@@ -389,7 +393,7 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, d
     const double d = std::sqrt(total);
     const double rinv = 1.0 / d;
     QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, int(target), res, d, rinv, reg->stream, reg->sms,
-                                reg->zmask, reg->zval),
+                                reg->zmask, reg->zval, exact_quotient(reg)),
             "collapse");
     record_outcome(reg, target, res);
     if (outcome) *outcome = res;
@@ -429,12 +433,12 @@ int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const
         if (k + 1 < m && !seq) {
             QS_CUDA(qs::launch_collapse_probs(reg->state, reg->n, reg->prec, t, res, d, rinv, int(targets[k + 1]),
                                               reg->partials, kMaxPartials, reg->dres, reg->stream, reg->sms,
-                                              reg->zmask, reg->zval),
+                                              reg->zmask, reg->zval, exact_quotient(reg)),
                     "collapse_probs");
             record_outcome(reg, targets[k], res);
         } else {
             QS_CUDA(qs::launch_collapse(reg->state, reg->n, reg->prec, t, res, d, rinv, reg->stream, reg->sms,
-                                        reg->zmask, reg->zval),
+                                        reg->zmask, reg->zval, exact_quotient(reg)),
                     "collapse");
             record_outcome(reg, targets[k], res);
             if (k + 1 < m)

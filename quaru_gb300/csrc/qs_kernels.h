@@ -76,14 +76,16 @@ cudaError_t launch_measure_probs(const void* state, int n, int prec, int target,
                                  int max_partials, double* out, cudaStream_t s, int sms, uint64_t zmask = 0,
                                  uint64_t zval = 0, bool sequential = false);
 // Zero amplitudes whose target bit != outcome and divide the rest by d (rinv = 1/d), within the
-// live subspace.
+// live subspace: complex128 with exact_quotient as the correctly rounded quotient (Rust's `/`),
+// otherwise within one ulp of it (a multiply by rinv).
 cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
-                            cudaStream_t s, int sms, uint64_t zmask = 0, uint64_t zval = 0);
+                            cudaStream_t s, int sms, uint64_t zmask = 0, uint64_t zval = 0,
+                            bool exact_quotient = true);
 // The same collapse, with the probability sums of next_target over the kept amplitudes written to
 // out[0], out[1] (device) in the same pass.
 cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int outcome, double d, double rinv,
                                   int next_target, double* partials, int max_partials, double* out, cudaStream_t s,
-                                  int sms, uint64_t zmask, uint64_t zval);
+                                  int sms, uint64_t zmask, uint64_t zval, bool exact_quotient = true);
 // norm_sqr of amplitudes [first, first + count) into dst (device).
 cudaError_t launch_norm_sqr(const void* state, int prec, uint64_t first, uint64_t count, double* dst,
                             cudaStream_t s, int sms);

@@ -278,10 +278,17 @@ __device__ __forceinline__ double div_markstein(double x, double d, double rinv)
     return fma(r, rinv, q);
 }
 
+// How the kept amplitudes are divided by d = sqrt(total): the correctly rounded quotient (Markstein's
+// step; what Rust's `/` gives, for registers in the reference's arithmetic), a true division (when
+// RN(1/d) is not usable), or one multiply by RN(1/d), within one ulp of the quotient (registers in
+// the other arithmetic forms, held to 1e-14: GB300's FP64 pipe bounds a collapse, and this form
+// takes 2 FP64 operations per amplitude instead of 6).
+constexpr int kDivMarkstein = 0, kDivTrue = 1, kDivMul = 2;
+
 // The kept amplitude divided by sqrt(total) (src/register.rs:337), in the state's type.
-template <typename T, bool TRUEDIV>
+template <typename T, int DIV>
 __device__ __forceinline__ T collapse_value(T v, double d, double rinv, double2* as_double) {
-    if constexpr (sizeof(T) == 8 && !TRUEDIV) {
+    if constexpr (sizeof(T) == 8 && DIV != kDivTrue) {
         // complex64: one FP64 multiply by RN(1/d) per component, rounded to float on the integer
         // pipe (the quotient is stored as a float, so the exactly rounded double quotient of the
         // complex128 path buys nothing here)
@@ -292,9 +299,12 @@ __device__ __forceinline__ T collapse_value(T v, double d, double rinv, double2*
     } else {
         const double2 x = to_d2_int(v);
         double2 y;
-        if (TRUEDIV) {
+        if constexpr (DIV == kDivTrue) {
             y.x = x.x / d;
             y.y = x.y / d;
+        } else if constexpr (DIV == kDivMul) {
+            y.x = x.x * rinv;
+            y.y = x.y * rinv;
         } else {
             y.x = div_markstein(x.x, d, rinv);
             y.y = div_markstein(x.y, d, rinv);
@@ -306,7 +316,7 @@ __device__ __forceinline__ T collapse_value(T v, double d, double rinv, double2*
     }
 }
 
-template <typename T, bool TRUEDIV>
+template <typename T, int DIV>
 __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t npairs, uint64_t tb,
                                                  const __grid_constant__ IndexMap map, int outcome, double d,
                                                  double rinv) {
@@ -315,7 +325,7 @@ __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t np
         const uint64_t i0 = expand_index(t, map);
         const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
         double2 unused;
-        st[keep] = collapse_value<T, TRUEDIV>(st[keep], d, rinv, &unused);
+        st[keep] = collapse_value<T, DIV>(st[keep], d, rinv, &unused);
         st[drop] = T{0, 0};
     }
 }
@@ -323,7 +333,7 @@ __global__ void __launch_bounds__(kT) k_collapse(T* __restrict__ st, uint64_t np
 // The collapse of one measurement fused with the probability sums of the next one (measure_circuit,
 // src/register.rs:371-377): the kept amplitudes, once divided, are the only non-zero amplitudes the
 // next target sees, so their squares are summed by that target's bit in the same pass.
-template <typename T, bool TRUEDIV>
+template <typename T, int DIV>
 __global__ void __launch_bounds__(kT) k_collapse_probs(T* __restrict__ st, uint64_t npairs, uint64_t tb,
                                                        const __grid_constant__ IndexMap map, int outcome, double d,
                                                        double rinv, uint64_t next_tb, double* __restrict__ partials) {
@@ -333,7 +343,7 @@ __global__ void __launch_bounds__(kT) k_collapse_probs(T* __restrict__ st, uint6
         const uint64_t i0 = expand_index(t, map);
         const uint64_t keep = outcome ? (i0 | tb) : i0, drop = outcome ? i0 : (i0 | tb);
         double2 y;
-        st[keep] = collapse_value<T, TRUEDIV>(st[keep], d, rinv, &y);
+        st[keep] = collapse_value<T, DIV>(st[keep], d, rinv, &y);
         st[drop] = T{0, 0};
         const double q = fma(y.x, y.x, y.y * y.y);
         if (keep & next_tb)
@@ -348,55 +358,66 @@ __global__ void __launch_bounds__(kT) k_collapse_probs(T* __restrict__ st, uint6
     }
 }
 
-static bool use_truediv(double d, double rinv) {
-    // Markstein's step needs a finite reciprocal of a normal divisor.
-    return !(std::isfinite(rinv) && d > 1e-300 && std::isfinite(d));
+static int div_mode(double d, double rinv, bool exact_quotient) {
+    // Markstein's step and the multiply need a finite reciprocal of a normal divisor.
+    if (!(std::isfinite(rinv) && d > 1e-300 && std::isfinite(d))) return kDivTrue;
+    return exact_quotient ? kDivMarkstein : kDivMul;
+}
+
+template <typename T, int DIV>
+static void collapse_t(void* state, uint64_t npairs, uint64_t tb, const IndexMap& map, int outcome, double d,
+                       double rinv, int grid, cudaStream_t s) {
+    k_collapse<T, DIV><<<grid, kT, 0, s>>>((T*)state, npairs, tb, map, outcome, d, rinv);
+}
+
+template <typename T, int DIV>
+static void collapse_probs_t(void* state, uint64_t npairs, uint64_t tb, const IndexMap& map, int outcome, double d,
+                             double rinv, uint64_t ntb, double* partials, int grid, cudaStream_t s) {
+    k_collapse_probs<T, DIV><<<grid, kT, 0, s>>>((T*)state, npairs, tb, map, outcome, d, rinv, ntb, partials);
 }
 
 cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcome, double d, double rinv,
-                            cudaStream_t s, int sms, uint64_t zmask, uint64_t zval) {
+                            cudaStream_t s, int sms, uint64_t zmask, uint64_t zval, bool exact_quotient) {
     const IndexMap map = subspace_map(target, zmask, zval);
     const uint64_t npairs = subspace_pairs(n, target, zmask);
     const uint64_t tb = 1ull << target;
     const int grid = grid_cap(npairs, sms, 2);
-    const bool truediv = use_truediv(d, rinv);
-    if (prec == QS_PREC_C64) {
-        if (truediv)
-            k_collapse<float2, true><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv);
+    const int mode = div_mode(d, rinv, exact_quotient);
+    if (prec == QS_PREC_C64) {  // complex64 multiplies by RN(1/d) unless it must divide
+        if (mode == kDivTrue)
+            collapse_t<float2, kDivTrue>(state, npairs, tb, map, outcome, d, rinv, grid, s);
         else
-            k_collapse<float2, false><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv);
+            collapse_t<float2, kDivMul>(state, npairs, tb, map, outcome, d, rinv, grid, s);
+    } else if (mode == kDivTrue) {
+        collapse_t<double2, kDivTrue>(state, npairs, tb, map, outcome, d, rinv, grid, s);
+    } else if (mode == kDivMul) {
+        collapse_t<double2, kDivMul>(state, npairs, tb, map, outcome, d, rinv, grid, s);
     } else {
-        if (truediv)
-            k_collapse<double2, true><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv);
-        else
-            k_collapse<double2, false><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv);
+        collapse_t<double2, kDivMarkstein>(state, npairs, tb, map, outcome, d, rinv, grid, s);
     }
     return counted(cudaGetLastError());
 }
 
 cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int outcome, double d, double rinv,
                                   int next_target, double* partials, int max_partials, double* out, cudaStream_t s,
-                                  int sms, uint64_t zmask, uint64_t zval) {
+                                  int sms, uint64_t zmask, uint64_t zval, bool exact_quotient) {
     const IndexMap map = subspace_map(target, zmask, zval);
     const uint64_t npairs = subspace_pairs(n, target, zmask);
     const uint64_t tb = 1ull << target, ntb = 1ull << next_target;
     int grid = grid_cap(npairs, sms, 2);
     if (grid > max_partials) grid = max_partials;
-    const bool truediv = use_truediv(d, rinv);
+    const int mode = div_mode(d, rinv, exact_quotient);
     if (prec == QS_PREC_C64) {
-        if (truediv)
-            k_collapse_probs<float2, true><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv, ntb,
-                                                                partials);
+        if (mode == kDivTrue)
+            collapse_probs_t<float2, kDivTrue>(state, npairs, tb, map, outcome, d, rinv, ntb, partials, grid, s);
         else
-            k_collapse_probs<float2, false><<<grid, kT, 0, s>>>((float2*)state, npairs, tb, map, outcome, d, rinv, ntb,
-                                                                 partials);
+            collapse_probs_t<float2, kDivMul>(state, npairs, tb, map, outcome, d, rinv, ntb, partials, grid, s);
+    } else if (mode == kDivTrue) {
+        collapse_probs_t<double2, kDivTrue>(state, npairs, tb, map, outcome, d, rinv, ntb, partials, grid, s);
+    } else if (mode == kDivMul) {
+        collapse_probs_t<double2, kDivMul>(state, npairs, tb, map, outcome, d, rinv, ntb, partials, grid, s);
     } else {
-        if (truediv)
-            k_collapse_probs<double2, true><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv,
-                                                                 ntb, partials);
-        else
-            k_collapse_probs<double2, false><<<grid, kT, 0, s>>>((double2*)state, npairs, tb, map, outcome, d, rinv,
-                                                                  ntb, partials);
+        collapse_probs_t<double2, kDivMarkstein>(state, npairs, tb, map, outcome, d, rinv, ntb, partials, grid, s);
     }
     k_prob_final<<<1, kT, 0, s>>>(partials, grid, out);
     return counted(cudaGetLastError(), 2);
