@@ -60,8 +60,9 @@ namespace qs {
 namespace {
 
 constexpr int kOzMathWarps = 16;
-constexpr int kOzMath = 32 * kOzMathWarps;   // math threads; the MMA warp follows them
-constexpr int kOzThreads = kOzMath + 32;
+constexpr int kOzMath = 32 * kOzMathWarps;   // math threads; the two MMA warps follow them
+constexpr int kOzIssuers = 2;                // MMA warps: levels 0..4, and the tail (levels 5..6)
+constexpr int kOzThreads = kOzMath + 32 * kOzIssuers;
 constexpr int kOzRows = 8;                   // block rows per math thread
 constexpr int kOzAcc = 6;                    // accumulators: levels 0..4, then 5..6
 constexpr int kOzSlots = 4;                  // A slots in tensor memory
@@ -173,21 +174,24 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, 
 }
 
 // The MMAs of A slice S (tensor-memory columns from aslot) against every B slice t with S + t <= 6
-// (descriptor of B slice 0: bdesc0; slice t and K step ks start (8192 t + 256 ks) bytes further, an
-// offset the descriptor's 14-bit start-address field absorbs without carry), into the level
-// accumulators; a tile's first slice starts levels 0..5 afresh. Unrolled per slice, so every
-// offset and accumulate flag is a constant.
-template <int S>
+// whose level accumulator belongs to MMA warp ISSUER: issuer 0 levels 0..4, issuer 1 the tail
+// (levels 5..6). Each accumulator has one issuer, so its MMAs keep their order (the reset first,
+// then the accumulations). Descriptor of B slice 0: bdesc0; slice t and K step ks start
+// (8192 t + 256 ks) bytes further, an offset the descriptor's 14-bit start-address field absorbs
+// without carry. A tile's first slice starts levels 0..5 afresh (level 5 at t = 5, before t = 6
+// adds to it). K step outermost, so consecutive MMAs go to different accumulators. Unrolled per
+// slice: every offset and accumulate flag is a constant.
+template <int S, int ISSUER>
 __device__ __forceinline__ void oz_issue_slice(uint32_t tmem, uint32_t aslot, uint64_t bdesc0) {
     constexpr uint32_t idesc = tc_idesc_bf16(128, 64);
 #pragma unroll
-    for (int t = 0; t + S < kOzSlices; t++) {
-        const uint32_t acc = tmem + 64u * uint32_t(min(S + t, kOzAcc - 1));
+    for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
 #pragma unroll
-        for (uint32_t ks = 0; ks < 4; ks++)  // K = 16 per MMA
-            tc_mma_f16_ta(acc, aslot + 8u * ks, bdesc0 + ((uint64_t(t) * kOzSliceBytes + 256u * ks) >> 4), idesc,
-                          (S > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
-    }
+        for (int t = 0; t + S < kOzSlices; t++)
+            if ((S + t < kOzAcc - 1) == (ISSUER == 0))
+                tc_mma_f16_ta(tmem + 64u * uint32_t(min(S + t, kOzAcc - 1)), aslot + 8u * ks,
+                              bdesc0 + ((uint64_t(t) * kOzSliceBytes + 256u * ks) >> 4), idesc,
+                              (S > 0 || ks > 0 || t == kOzSlices - 1) ? 1u : 0u);
 }
 
 // Wait for the phase of `parity` with short sleeps between polls (the math warps: their polls would
@@ -282,17 +286,17 @@ __global__ void __launch_bounds__(kOzThreads, 1)
             if (r >> b & 1) o |= 1ull << sa.rhigh[b];
         rowoff[r] = o;
     }
-    if (warp == kOzMathWarps) tc_alloc(tslot, kOzTmemCols);
+    if (warp == kOzMathWarps) tc_alloc(tslot, kOzTmemCols);  // the first MMA warp
     if (tid == 0) {
         mbar_init(&bars[kBarB], 1);
         for (int b = 0; b < 2; b++) mbar_init(&bars[kBarLoad + b], kOzMath);
         for (int j = 0; j < kOzSlots; j++) {
             mbar_init(&bars[kBarFull + j], kOzMathWarps);
-            mbar_init(&bars[kBarFree + j], 1);
+            mbar_init(&bars[kBarFree + j], kOzIssuers);  // one commit per MMA warp
         }
-        mbar_init(&bars[kBarAccFull], 1);
+        mbar_init(&bars[kBarAccFull], kOzIssuers);
         mbar_init(&bars[kBarAccFree], kOzMathWarps);
-        mbar_init(&bars[kBarDone], 1);
+        mbar_init(&bars[kBarDone], kOzIssuers);
         fence_mbar_init();
         s_abort = 0;
     }
@@ -337,8 +341,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     const uint64_t nmy = ntiles > first ? (ntiles - 1 - first) / stride + 1 : 0;
     const uint32_t rmask = (1u << sa.RL) - 1u;
 
-    if (warp == kOzMathWarps) {
-        // ---- the MMA warp: slice s of a tile against every B slice t with s + t <= 6
+    if (warp >= kOzMathWarps) {
+        // ---- the MMA warps: slice s of a tile against every B slice t with s + t <= 6, issuer 0 into
+        // levels 0..4 (60 MMAs per tile), issuer 1 into the tail (52), each on its own scheduler
+        const int issuer = warp - kOzMathWarps;
         if (lane == 0) {
             bool ok = s_abort == 0;
             const uint64_t bdesc0 = tc_smem_desc(saddr(sB), 128u, 1024u);
@@ -358,13 +364,13 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                     tc_fence_after();
                     const uint32_t aslot = tmem + kOzASlot + 32u * slot;
                     switch (s) {
-                        case 0: oz_issue_slice<0>(tmem, aslot, bdesc0); break;
-                        case 1: oz_issue_slice<1>(tmem, aslot, bdesc0); break;
-                        case 2: oz_issue_slice<2>(tmem, aslot, bdesc0); break;
-                        case 3: oz_issue_slice<3>(tmem, aslot, bdesc0); break;
-                        case 4: oz_issue_slice<4>(tmem, aslot, bdesc0); break;
-                        case 5: oz_issue_slice<5>(tmem, aslot, bdesc0); break;
-                        default: oz_issue_slice<6>(tmem, aslot, bdesc0); break;
+                        case 0: issuer ? oz_issue_slice<0, 1>(tmem, aslot, bdesc0) : oz_issue_slice<0, 0>(tmem, aslot, bdesc0); break;
+                        case 1: issuer ? oz_issue_slice<1, 1>(tmem, aslot, bdesc0) : oz_issue_slice<1, 0>(tmem, aslot, bdesc0); break;
+                        case 2: issuer ? oz_issue_slice<2, 1>(tmem, aslot, bdesc0) : oz_issue_slice<2, 0>(tmem, aslot, bdesc0); break;
+                        case 3: issuer ? oz_issue_slice<3, 1>(tmem, aslot, bdesc0) : oz_issue_slice<3, 0>(tmem, aslot, bdesc0); break;
+                        case 4: issuer ? oz_issue_slice<4, 1>(tmem, aslot, bdesc0) : oz_issue_slice<4, 0>(tmem, aslot, bdesc0); break;
+                        case 5: issuer ? oz_issue_slice<5, 1>(tmem, aslot, bdesc0) : oz_issue_slice<5, 0>(tmem, aslot, bdesc0); break;
+                        default: issuer ? oz_issue_slice<6, 1>(tmem, aslot, bdesc0) : oz_issue_slice<6, 0>(tmem, aslot, bdesc0); break;
                     }
                     tc_commit(&bars[kBarFree + slot]);
                     if (s == kOzSlices - 1) tc_commit(&bars[kBarAccFull]);
