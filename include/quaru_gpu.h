@@ -171,7 +171,9 @@ int qs_apply_circuit(qs_register* reg, const qs_gate* gates, size_t m,
  * QS_ARITH_EXACT with n <= 20 add the squares in index order as the reference
  * does (:306-315), so sums, outcome and collapsed state are bit-identical to
  * it; larger registers and the other forms use a fixed-order parallel tree
- * (within 1e-14). The collapse divides by sqrt(prob) correctly rounded (:337).
+ * (within 1e-14). The collapse divides by sqrt(prob) (:337): correctly rounded
+ * on complex128 registers in QS_ARITH_EXACT, as Rust's `/`; the other forms
+ * multiply by the rounded reciprocal (within one ulp of the quotient).
  * Qubits measured since their last gate stay collapsed: later measurements
  * read only the amplitudes that can still be non-zero. */
 int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
