@@ -185,7 +185,13 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
  * before any work (InvalidTarget, err[2] = its index). Each collapse pass also
  * sums the next target's probabilities over the kept amplitudes, and each pass
  * reads only the live subspace, so measuring all n qubits costs about two
- * sweeps of the state instead of 2n. */
+ * sweeps of the state instead of 2n. Three or more distinct targets on a
+ * register of 14 qubits or more with no measurement recorded since its last
+ * gate run on a compact copy of the live subspace (a scratch buffer of half
+ * the state, allocated by the register's first such sequence and kept until
+ * qs_destroy; without the memory the passes stay in place), with results bit
+ * for bit those of the in-place passes; QS_MEASURE_COMPACT=off keeps them in
+ * place. */
 int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
                         double* prob0s, double* prob1s, size_t* err);
 

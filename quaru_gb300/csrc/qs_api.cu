@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -37,6 +38,9 @@ struct qs_register {
     // differ from zval is an exact zero, so later measurements visit only the live subspace.
     uint64_t zmask = 0;
     uint64_t zval = 0;
+    // Scratch of the compact measurement sequences (half the state), allocated by the first one and
+    // kept until the register is destroyed.
+    void* mscratch = nullptr;
 };
 
 namespace qs {
@@ -134,6 +138,7 @@ void destroy(qs_register* r) {
     if (r->state) cudaFree(r->state);
     if (r->partials) cudaFree(r->partials);
     if (r->dres) cudaFree(r->dres);
+    if (r->mscratch) cudaFree(r->mscratch);
     if (r->hres) cudaFreeHost(r->hres);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
@@ -402,6 +407,95 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome, d
     return QS_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// A sequence of three or more distinct targets on a register of 14 qubits or more with no
+// measurement recorded runs on a compact copy of the live subspace (launch_collapse_compact): the
+// first collapse copies the kept half of the state, divided, into a half-size scratch buffer (the
+// register's, allocated by its first such sequence and kept: allocating and mapping half a large
+// state on every call costs milliseconds), later
+// passes halve the live data between that buffer and the front of the state buffer, and at the end
+// the state is zeroed (the value the in-place passes leave in every dropped amplitude) and the last
+// live amplitudes are written back to their places. Results are bit-identical to the in-place
+// passes; a pass moves its live data instead of whole DRAM sectors of a strided subspace. Returns 1
+// when the scratch buffer cannot be allocated, and the caller then runs the in-place passes.
+constexpr int kCompactMinQubits = 14;
+
+int measure_sequence_compact(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
+                             double* prob0s, double* prob1s) {
+    const int n = reg->n;
+    const size_t amp = amp_bytes(reg->prec);
+    if (!reg->mscratch && cudaMalloc(&reg->mscratch, (size_t(1) << (n - 1)) * amp) != cudaSuccess) {
+        cudaGetLastError();
+        reg->mscratch = nullptr;
+        return 1;
+    }
+    void* scratch = reg->mscratch;
+    const bool exactq = exact_quotient(reg);
+    QS_CUDA(qs::launch_measure_probs(reg->state, n, reg->prec, int(targets[0]), reg->partials, kMaxPartials,
+                                     reg->dres, reg->stream, reg->sms),
+            "measure_probs");
+    std::vector<int> free_bits(n);  // the source buffer's index bits, as qubits, ascending
+    for (int q = 0; q < n; q++) free_bits[q] = q;
+    auto index_of = [&](size_t q) {
+        return int(std::find(free_bits.begin(), free_bits.end(), int(q)) - free_bits.begin());
+    };
+    const void* src = reg->state;
+    void* dst = nullptr;
+    for (size_t k = 0; k < m; k++) {
+        QS_CUDA(cudaMemcpyAsync(reg->hres, reg->dres, 2 * sizeof(double), cudaMemcpyDeviceToHost, reg->stream),
+                "measure readback");
+        QS_CUDA(cudaStreamSynchronize(reg->stream), "measure sync");
+        const double p0 = reg->hres[0], p1 = reg->hres[1];
+        const int res = draws[k] > p0 ? 1 : 0;  // src/register.rs:321
+        const double total = res ? p1 : p0;
+        const double d = std::sqrt(total);
+        const double rinv = 1.0 / d;
+        const int nfree = int(free_bits.size());
+        const int pos = index_of(targets[k]);
+        free_bits.erase(free_bits.begin() + pos);
+        const int next_pos = k + 1 < m ? index_of(targets[k + 1]) : -1;
+        dst = (k % 2 == 0) ? scratch : reg->state;  // the first pass reads the whole state
+        QS_CUDA(qs::launch_collapse_compact(src, dst, nfree, reg->prec, pos, res, d, rinv, next_pos, reg->partials,
+                                            kMaxPartials, reg->dres, reg->stream, reg->sms, exactq),
+                "collapse_compact");
+        record_outcome(reg, targets[k], res);
+        src = dst;
+        outcomes[k] = res;
+        if (prob0s) prob0s[k] = p0;
+        if (prob1s) prob1s[k] = p1;
+    }
+    const size_t live = size_t(1) << free_bits.size();
+    if (dst == reg->state)
+        QS_CUDA(cudaMemcpyAsync(scratch, reg->state, live * amp, cudaMemcpyDeviceToDevice, reg->stream),
+                "compact copy");
+    QS_CUDA(cudaMemsetAsync(reg->state, 0, (size_t(1) << n) * amp, reg->stream), "state zero");
+    QS_CUDA(qs::launch_scatter_live(reg->state, scratch, n, reg->prec, reg->zmask, reg->zval, reg->stream, reg->sms),
+            "scatter live");
+    return QS_OK;
+}
+
+// QS_MEASURE_COMPACT=off keeps every measurement pass in place (for comparing the two forms).
+bool compact_measurement_enabled() {
+    const char* v = std::getenv("QS_MEASURE_COMPACT");
+    return !(v && (std::strcmp(v, "off") == 0 || std::strcmp(v, "0") == 0));
+}
+
+bool distinct_targets(const size_t* targets, size_t m) {
+    uint64_t seen = 0;
+    for (size_t k = 0; k < m; k++) {
+        if (seen >> targets[k] & 1ull) return false;
+        seen |= 1ull << targets[k];
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
 int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
                         double* prob0s, double* prob1s, size_t* err) {
     qs::TraceRange trace("qs_measure_sequence");
@@ -417,6 +511,11 @@ int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const
         }
     if (m == 0) return QS_OK;
     const bool seq = sequential_sums(reg);
+    if (!seq && m >= 3 && reg->zmask == 0 && reg->n >= kCompactMinQubits && distinct_targets(targets, m) &&
+        compact_measurement_enabled()) {
+        const int rc = measure_sequence_compact(reg, targets, m, draws, outcomes, prob0s, prob1s);
+        if (rc != 1) return rc;
+    }
     QS_CUDA(qs::launch_measure_probs(reg->state, reg->n, reg->prec, int(targets[0]), reg->partials, kMaxPartials,
                                      reg->dres, reg->stream, reg->sms, reg->zmask, reg->zval, seq),
             "measure_probs");

@@ -86,6 +86,19 @@ cudaError_t launch_collapse(void* state, int n, int prec, int target, int outcom
 cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int outcome, double d, double rinv,
                                   int next_target, double* partials, int max_partials, double* out, cudaStream_t s,
                                   int sms, uint64_t zmask, uint64_t zval, bool exact_quotient = true);
+// One pass of a measurement sequence on a compact buffer: `src` holds 2^nfree amplitudes indexed by
+// the free bits in ascending order; the amplitudes whose bit `pos` equals `outcome` are divided by d
+// (rinv = 1/d; correctly rounded with exact_quotient on complex128) and written densely to `dst`
+// (2^(nfree-1) amplitudes, bit pos removed). With next_pos >= 0, the probability sums of bit
+// next_pos of dst's index go to out[0], out[1] (device) in the same pass. Same pairs, order, grid and
+// arithmetic as launch_collapse_probs.
+cudaError_t launch_collapse_compact(const void* src, void* dst, int nfree, int prec, int pos, int outcome, double d,
+                                    double rinv, int next_pos, double* partials, int max_partials, double* out,
+                                    cudaStream_t s, int sms, bool exact_quotient);
+// Write the 2^(n - popcount(zmask)) amplitudes of `src` (indexed by the free bits) to their places in
+// the state: the bits of zmask set to those of zval.
+cudaError_t launch_scatter_live(void* state, const void* src, int n, int prec, uint64_t zmask, uint64_t zval,
+                                cudaStream_t s, int sms);
 // norm_sqr of amplitudes [first, first + count) into dst (device).
 cudaError_t launch_norm_sqr(const void* state, int prec, uint64_t first, uint64_t count, double* dst,
                             cudaStream_t s, int sms);

@@ -423,6 +423,105 @@ cudaError_t launch_collapse_probs(void* state, int n, int prec, int target, int 
     return counted(cudaGetLastError(), 2);
 }
 
+// ---------------------------------------------------------------- measurement on a compact subspace
+// A measurement sequence on a dense state (qs_measure_sequence): after the first collapse the live
+// amplitudes are strided through the state (the measured qubits' bits fixed), so in-place passes
+// move whole 32-byte sectors for every live 16-byte amplitude. Here each pass instead reads the
+// kept half of a buffer whose index runs over the free bits only and writes it, divided, densely
+// into the next buffer; the sums of the next target come from the same pass. Every pass visits the
+// pairs t in the order and with the grid of k_collapse_probs (the free bits in ascending order, the
+// target's bit inserted) and divides as it does, so the sums, outcomes and divided amplitudes are
+// bit for bit those of the in-place passes.
+template <typename T, int DIV, bool SUMS>
+__global__ void __launch_bounds__(kT) k_collapse_compact(const T* __restrict__ src, T* __restrict__ dst,
+                                                         uint64_t npairs, const __grid_constant__ IndexMap map,
+                                                         uint64_t keepbit, double d, double rinv, uint64_t next_bit,
+                                                         double* __restrict__ partials) {
+    const uint64_t stride = uint64_t(gridDim.x) * kT;
+    double p0 = 0.0, p1 = 0.0;
+    for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < npairs; t += stride) {
+        double2 y;
+        dst[t] = collapse_value<T, DIV>(src[expand_index(t, map) | keepbit], d, rinv, &y);
+        if constexpr (SUMS) {
+            const double q = fma(y.x, y.x, y.y * y.y);
+            if (t & next_bit)
+                p1 += q;
+            else
+                p0 += q;
+        }
+    }
+    if constexpr (SUMS) {
+        block_sum2(p0, p1);
+        if (threadIdx.x == 0) {
+            partials[2 * blockIdx.x] = p0;
+            partials[2 * blockIdx.x + 1] = p1;
+        }
+    }
+}
+
+template <typename T, int DIV>
+static void collapse_compact_t(const void* src, void* dst, uint64_t npairs, const IndexMap& map, uint64_t keepbit,
+                               double d, double rinv, int next_pos, double* partials, int grid, cudaStream_t s) {
+    if (next_pos >= 0)
+        k_collapse_compact<T, DIV, true><<<grid, kT, 0, s>>>((const T*)src, (T*)dst, npairs, map, keepbit, d, rinv,
+                                                             1ull << next_pos, partials);
+    else
+        k_collapse_compact<T, DIV, false><<<grid, kT, 0, s>>>((const T*)src, (T*)dst, npairs, map, keepbit, d, rinv,
+                                                              0ull, partials);
+}
+
+cudaError_t launch_collapse_compact(const void* src, void* dst, int nfree, int prec, int pos, int outcome, double d,
+                                    double rinv, int next_pos, double* partials, int max_partials, double* out,
+                                    cudaStream_t s, int sms, bool exact_quotient) {
+    const IndexMap map = subspace_map(pos, 0, 0);
+    const uint64_t npairs = 1ull << (nfree - 1);
+    const uint64_t keepbit = outcome ? (1ull << pos) : 0ull;
+    int grid = grid_cap(npairs, sms, 2);
+    if (next_pos >= 0 && grid > max_partials) grid = max_partials;  // the in-place pass's grid
+    const int mode = div_mode(d, rinv, exact_quotient);
+    if (prec == QS_PREC_C64) {
+        if (mode == kDivTrue)
+            collapse_compact_t<float2, kDivTrue>(src, dst, npairs, map, keepbit, d, rinv, next_pos, partials, grid, s);
+        else
+            collapse_compact_t<float2, kDivMul>(src, dst, npairs, map, keepbit, d, rinv, next_pos, partials, grid, s);
+    } else if (mode == kDivTrue) {
+        collapse_compact_t<double2, kDivTrue>(src, dst, npairs, map, keepbit, d, rinv, next_pos, partials, grid, s);
+    } else if (mode == kDivMul) {
+        collapse_compact_t<double2, kDivMul>(src, dst, npairs, map, keepbit, d, rinv, next_pos, partials, grid, s);
+    } else {
+        collapse_compact_t<double2, kDivMarkstein>(src, dst, npairs, map, keepbit, d, rinv, next_pos, partials, grid,
+                                                   s);
+    }
+    if (next_pos < 0) return counted(cudaGetLastError());
+    k_prob_final<<<1, kT, 0, s>>>(partials, grid, out);
+    return counted(cudaGetLastError(), 2);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kT) k_scatter_live(T* __restrict__ st, const T* __restrict__ src, uint64_t count,
+                                                     const __grid_constant__ IndexMap map) {
+    const uint64_t stride = uint64_t(gridDim.x) * kT;
+    for (uint64_t t = uint64_t(blockIdx.x) * kT + threadIdx.x; t < count; t += stride) st[expand_index(t, map)] = src[t];
+}
+
+cudaError_t launch_scatter_live(void* state, const void* src, int n, int prec, uint64_t zmask, uint64_t zval,
+                                cudaStream_t s, int sms) {
+    IndexMap map;
+    std::memset(&map, 0, sizeof(map));
+    int k = 0;
+    for (int b = 0; b < 64; b++)
+        if (zmask >> b & 1ull) map.pos[k++] = uint8_t(b);
+    map.npos = k;
+    map.fixval = zval & zmask;
+    const uint64_t count = 1ull << (n - k);
+    const int grid = grid_cap(count, sms, 2);
+    if (prec == QS_PREC_C64)
+        k_scatter_live<float2><<<grid, kT, 0, s>>>((float2*)state, (const float2*)src, count, map);
+    else
+        k_scatter_live<double2><<<grid, kT, 0, s>>>((double2*)state, (const double2*)src, count, map);
+    return counted(cudaGetLastError());
+}
+
 // ---------------------------------------------------------------- read-back
 // norm_sqr = re*re + im*im, rounded as num-complex computes it.
 template <typename T>

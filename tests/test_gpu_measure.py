@@ -124,3 +124,34 @@ def test_sequence_rejects_bad_targets_before_any_work():
     with pytest.raises(RuntimeError):
         g.measure_sequence([0, 4], [0.5, 0.5])
     assert value_equal(g.state, st)
+
+
+@pytest.mark.parametrize("n,arith,precision", [(17, 1, 0), (17, 2, 0), (17, 1, 1), (21, 0, 0)])
+def test_compact_sequence_bit_identical_to_in_place(monkeypatch, n, arith, precision):
+    """Sequences of three or more distinct targets on a register with no measurement recorded run on
+    a compact copy of the live subspace; QS_MEASURE_COMPACT=off keeps them in place. Both forms visit
+    the same pairs in the same order and divide the same way (the correctly rounded quotient for the
+    exact arithmetic, here above the 20 qubits of the reference-order sums), so outcomes, probability
+    sums and every amplitude of the final state (zeros included, by sign) agree bit for bit. Targets
+    in random order, low and high."""
+    import quaru_gb300 as q
+
+    rng = np.random.default_rng(500 + n + arith + 10 * precision)
+    st = _state(rng, n)
+    targets = [int(x) for x in rng.permutation(n)[:9]]
+    draws = [float(x) for x in rng.uniform(size=len(targets))]
+    runs = []
+    for mode in ("on", "off"):
+        monkeypatch.setenv("QS_MEASURE_COMPACT", mode)
+        g = q.Register.from_int(n, 0, precision=precision)
+        g.set_arith(arith)
+        g.state = st
+        out = g.measure_sequence(targets, draws)
+        runs.append((out, g.last_sequence_probs, g.state))
+    (oa, pa, sa), (ob, pb, sb) = runs
+    assert oa == ob
+    assert pa == pb
+    assert np.array_equal(sa.view(np.uint64), sb.view(np.uint64))  # read back as complex128
+    # the live amplitudes survive: 2^(n - 9) of them, each |a|^2 summing to 1
+    assert np.count_nonzero(sa) == 1 << (n - len(targets))
+    assert math.isclose(float(np.sum(np.abs(sa) ** 2)), 1.0, rel_tol=1e-6 if precision else 1e-13)
