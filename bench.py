@@ -794,7 +794,7 @@ def run_kernels(args) -> None:
     init (basis and product state), dense 1-qubit (exact, FMA, DF64, fixed point; complex64),
     CNOT/permutation, dense 3-qubit, 6-qubit permutation and dense gates, probability reduction,
     read-back and collapse (both precisions), measurement sequences (fused collapse + next sums;
-    reference-order sums), stages (complex128 FMA tiles, complex128 FP64-accurate tensor-core blocks,
+    the compact live subspace; reference-order sums), stages (complex128 FMA tiles, complex128 FP64-accurate tensor-core blocks,
     complex64 register passes, complex64 3xTF32 tensor-core blocks), adjoint (FP64 and mixed), batch
     (FP64 and mixed)."""
     import quaru_gb300 as q
@@ -818,6 +818,11 @@ def run_kernels(args) -> None:
         r.try_apply_fast(O.Operation(u3, [0, n // 2, n - 3]))
         r.measure(n - 1, 0.5)
         r.measure_sequence([0, 1, n // 2], [0.3, 0.6, 0.4])  # fused collapse + next sums, live subspace
+        fresh = q.Register.from_int(n, 0)  # no measurement recorded: a sequence on the compact live subspace
+        fresh.set_arith(q.QS_ARITH_FMA)
+        fresh.apply_gates(layers[: n + n // 2])
+        fresh.measure_sequence([0, 3, n // 2, n - 1], [0.3, 0.6, 0.4, 0.7])
+        del fresh
         small = q.Register.from_int(12, 0)  # exact arithmetic: the reference's summation order
         small.apply_gates(layers[:12] if n == 12 else flatten(layered_circuit(12, 1, 7)))
         small.measure_sequence(list(range(12)), [0.5] * 12)
