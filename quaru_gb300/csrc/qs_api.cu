@@ -415,12 +415,12 @@ namespace {
 // measurement recorded runs on a compact copy of the live subspace (launch_collapse_compact): the
 // first collapse copies the kept half of the state, divided, into a half-size scratch buffer (the
 // register's, allocated by its first such sequence and kept: allocating and mapping half a large
-// state on every call costs milliseconds), later
-// passes halve the live data between that buffer and the front of the state buffer, and at the end
-// the state is zeroed (the value the in-place passes leave in every dropped amplitude) and the last
-// live amplitudes are written back to their places. Results are bit-identical to the in-place
-// passes; a pass moves its live data instead of whole DRAM sectors of a strided subspace. Returns 1
-// when the scratch buffer cannot be allocated, and the caller then runs the in-place passes.
+// state on every call costs milliseconds), later passes halve the live data between that buffer
+// and the front of the state buffer, and at the end the state is zeroed (the value the in-place
+// passes leave in every dropped amplitude) and the last live amplitudes are written back to their
+// places. Results are bit-identical to the in-place passes; a pass moves its live data instead of
+// whole DRAM sectors of a strided subspace. Returns 1 when the scratch buffer cannot be allocated,
+// and the caller then runs the in-place passes.
 constexpr int kCompactMinQubits = 14;
 
 int measure_sequence_compact(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
