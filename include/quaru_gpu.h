@@ -191,7 +191,8 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
  * the state, allocated by the register's first such sequence and kept until
  * qs_destroy; without the memory the passes stay in place), with results bit
  * for bit those of the in-place passes; QS_MEASURE_COMPACT=off keeps them in
- * place. */
+ * place. A call that fails with QS_CUDA_ERROR partway leaves the register's
+ * state unspecified. */
 int qs_measure_sequence(qs_register* reg, const size_t* targets, size_t m, const double* draws, int* outcomes,
                         double* prob0s, double* prob1s, size_t* err);
 
