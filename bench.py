@@ -270,6 +270,23 @@ def dense1_forms(q, torch, reg, layers, n: int, peak: float, count: int = 8) -> 
     return out
 
 
+def slowest_rank_seconds(dist, seconds: list, device: str) -> list:
+    """Each timing's maximum over all ranks (one all-reduce): a job of replicas takes as long as its
+    slowest rank. `dist` is None on a single process."""
+    import torch
+
+    t = torch.tensor(seconds, dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def job_gbs(rank_bytes: float, world: int, seconds: float) -> float:
+    """Whole-job GB/s of `world` replicas that each moved `rank_bytes` over the timed steps, in
+    `seconds` (the slowest rank's time for those steps)."""
+    return rank_bytes * world / seconds / 1e9
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -472,13 +489,9 @@ def run_ours(args) -> None:
     adjoint = None if args.no_adjoint else adjoint_section(q, torch, args)
     batch = None if args.no_batch else batch_section(q, args)
 
-    t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_s, e2e_s = float(t[0]), float(t[1])
-    total_bytes = step_bytes * world
-    value = total_bytes / dev_s / 1e9
-    e2e = total_bytes / e2e_s / 1e9
+    dev_s, e2e_s = slowest_rank_seconds(dist, [dev_s, e2e_s], "cuda")
+    value = job_gbs(step_bytes, world, dev_s)
+    e2e = job_gbs(step_bytes, world, e2e_s)
 
     haar_ms = [a.elapsed_time(b) for a, b in haar_events]
     avg_haar_s = statistics.mean(haar_ms) / 1e3 if haar_ms else float("nan")
