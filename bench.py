@@ -42,7 +42,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "30-qubit gate-sweep HBM GB/s"
 UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
-FP64_PEAK_TFLOPS_MEASURED = 1.194  # FP64 FMA rate measured on this machine's GB300 (8 independent chains/thread)
+FP64_PEAK_TFLOPS_MEASURED = 1.194  # FP64 FMA rate measured on a GB300 (8 independent chains/thread)
 
 
 def gate_bytes(op, n: int, amp_bytes: int) -> float:

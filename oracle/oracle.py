@@ -1,8 +1,8 @@
 """ctypes bindings of the CPU oracle (quaru_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline leg use this module as the checker. The product (quaru_gb300) never
-imports it.
+baseline leg use this module, as the oracle the GPU results are compared with.
+The product (quaru_gb300) never imports it.
 """
 from __future__ import annotations
 

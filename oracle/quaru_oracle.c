@@ -1,8 +1,8 @@
 /*
  * quaru_oracle.c — CPU oracle for the Quaru register path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU engine, never part of the
- * product. Plain-C restatement of DATX11-22/quaru src/register.rs (cited per
+ * TEST INFRASTRUCTURE ONLY: the oracle for the GPU engine's results, never part
+ * of the product. Plain-C restatement of DATX11-22/quaru src/register.rs (cited per
  * function), compiled with -O2 -ffp-contract=off so every floating-point
  * operation rounds exactly where the Rust code rounds (Rust never contracts
  * a*b+c into a fused multiply-add).

@@ -2,8 +2,8 @@
  * quaru_oracle.h — CPU oracle for the Quaru register path.
  *
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference
- * algorithm (DATX11-22/quaru, src/register.rs) used as the checker for the
- * GPU engine. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * algorithm (DATX11-22/quaru, src/register.rs), the oracle the GPU engine's
+ * results are compared with. Only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may load it. The product library never links or calls it.
  *
  * Parity status: pinned by the reference's own known-answer tests

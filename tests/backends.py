@@ -1,6 +1,6 @@
 """Two implementations of Quaru's Register API for the shared test suite.
 
-"oracle": the CPU restatement in oracle/ (the checker).
+"oracle": the CPU restatement of the reference algorithm in oracle/.
 "gpu":    quaru_gb300.Register (the product), on the GB300.
 Both expose new/from_int/try_from_qubits/apply/try_apply_fast/apply_all/
 try_apply_all/measure(target, draw)/state/size/clone; errors carry .code and
