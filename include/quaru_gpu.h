@@ -189,7 +189,7 @@ int qs_try_measure(qs_register* reg, size_t target, double draw, int* outcome,
  * register of 14 qubits or more with no measurement recorded since its last
  * gate run on a compact copy of the live subspace (a scratch buffer of half
  * the state, allocated by the register's first such sequence and kept until
- * qs_destroy; without the memory the passes stay in place), with results bit
+ * qs_register_free; without the memory the passes stay in place), with results bit
  * for bit those of the in-place passes; QS_MEASURE_COMPACT=off keeps them in
  * place. A call that fails with QS_CUDA_ERROR partway leaves the register's
  * state unspecified. */
