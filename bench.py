@@ -163,12 +163,12 @@ def cpu_layers_gbps(n: int, layers, budget_s: float | None = None, limit_s: floa
             "gbps": nbytes / el / 1e9, "completed": completed}
 
 
-def cpu_c1_seconds() -> dict:
+def cpu_parity_circuit_seconds() -> dict:
     """The 12-qubit, 200-gate parity configuration on the oracle, measuring every qubit."""
     from oracle.oracle import OracleRegister
-    from quaru_gb300.workloads import config1_circuit
+    from quaru_gb300.workloads import parity_circuit
 
-    c = config1_circuit()
+    c = parity_circuit()
     t0 = time.perf_counter()
     reg = OracleRegister.from_int(c.n, 0)
     for g in c.gates:
@@ -179,12 +179,12 @@ def cpu_c1_seconds() -> dict:
 
 def cpu_sweep(limit_s: float, start: int = 12, stop: int = 30) -> dict:
     """The family at n = start, start+2, ... (40 layers each) until a size runs past limit_s."""
-    from quaru_gb300.workloads import layered_circuit, seed_for
+    from quaru_gb300.workloads import layered_circuit, workload_seed
 
     runs = []
     largest = None
     for n in range(start, stop + 1, 2):
-        r = cpu_layers_gbps(n, layered_circuit(n, CPU_SWEEP_LAYERS, seed_for(2)), limit_s=limit_s)
+        r = cpu_layers_gbps(n, layered_circuit(n, CPU_SWEEP_LAYERS, workload_seed("layered_28q")), limit_s=limit_s)
         runs.append(r)
         if not r["completed"]:
             break
@@ -207,10 +207,10 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from quaru_gb300.workloads import layered_circuit, seed_for
+    from quaru_gb300.workloads import layered_circuit, workload_seed
 
     n = args.cpu_qubits
-    layers = layered_circuit(n, args.warmup + args.steps, seed_for(3))
+    layers = layered_circuit(n, args.warmup + args.steps, workload_seed("layered_30q"))
     cpu_layers_gbps(n, layers[: args.warmup])  # warm-up layers, untimed
     r = cpu_layers_gbps(n, layers[args.warmup:])
     value = r["gbps"]
@@ -230,7 +230,7 @@ def run_reference(args) -> None:
 
 
 def run_cpu_sweep(args) -> None:
-    out = {"cpu_sweep": cpu_sweep(args.cpu_limit), "c1": cpu_c1_seconds(), "cores": 1,
+    out = {"cpu_sweep": cpu_sweep(args.cpu_limit), "parity_12q": cpu_parity_circuit_seconds(), "cores": 1,
            "host_cpus": os.cpu_count(), "machine": os.uname().machine}
     print(json.dumps(out), flush=True)
 
@@ -302,7 +302,7 @@ def run_ours(args) -> None:
 
     import quaru_gb300 as q
     from quaru_gb300 import _lib
-    from quaru_gb300.workloads import layered_circuit, seed_for
+    from quaru_gb300.workloads import layered_circuit, workload_seed
 
     lib = _lib.load()
     n = args.qubits
@@ -310,7 +310,7 @@ def run_ours(args) -> None:
     prec = q.QS_PREC_C64 if args.precision == "c64" else q.QS_PREC_C128
     amp = 8 if prec == q.QS_PREC_C64 else 16
     nlayers = max(args.warmup + args.steps, 1)
-    layers = layered_circuit(n, min(nlayers, 40), seed_for(3))
+    layers = layered_circuit(n, min(nlayers, 40), workload_seed("layered_30q"))
     reg = q.Register.from_int(n, 0, precision=prec)
     reg.set_arith(arith)
     stream = torch.cuda.ExternalStream(reg.stream)
@@ -509,10 +509,10 @@ def run_ours(args) -> None:
     if world == 1 and not args.no_cpu:
         # the same sample as `--impl reference`: whole layers at CPU_QUBITS qubits, same seed
         n_cpu = args.cpu_qubits
-        r = cpu_layers_gbps(n_cpu, layered_circuit(n_cpu, 40, seed_for(3)), budget_s=args.cpu_budget)
+        r = cpu_layers_gbps(n_cpu, layered_circuit(n_cpu, 40, workload_seed("layered_30q")), budget_s=args.cpu_budget)
         cpu = {"value": r["gbps"], "unit": UNIT, "cores": 1, "kind": "port", "sample": cpu_sample_text(n_cpu, r),
                "gates_per_s": r["gates_per_s"], "host_cpus": os.cpu_count(),
-               "sweep": cpu_sweep(args.cpu_limit, stop=n_cpu), "c1": cpu_c1_seconds()}
+               "sweep": cpu_sweep(args.cpu_limit, stop=n_cpu), "parity_12q": cpu_parity_circuit_seconds()}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -571,9 +571,9 @@ def measure_section(q, torch, args) -> dict:
     reference-order sums), and measuring all qubits of a dense 30-qubit complex128 state as one
     sequence (each pass reads only the live subspace and fuses the next qubit's sums) against one
     qs_try_measure call per qubit."""
-    from quaru_gb300.workloads import config1_circuit, flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, parity_circuit, workload_seed
 
-    c = config1_circuit()
+    c = parity_circuit()
     reps = []
     for _ in range(5):
         t0 = time.perf_counter()
@@ -583,12 +583,12 @@ def measure_section(q, torch, args) -> dict:
         bits = r.measure_sequence(list(range(c.n)), c.draws)
         reps.append(time.perf_counter() - t0)
         del r
-    out = {"c1": {"workload": "12 qubits, 200 gates, measure all 12 (seeded draws)", "ms": 1e3 * min(reps),
-                  "bitstring": "".join(str(int(b)) for b in bits)}}
+    out = {"parity_12q": {"workload": "12 qubits, 200 gates, measure all 12 (seeded draws)", "ms": 1e3 * min(reps),
+                          "bitstring": "".join(str(int(b)) for b in bits)}}
     n = args.qubits
     a = q.Register.from_int(n, 0)
     a.set_arith(q.QS_ARITH_FMA)
-    a.apply_gates(flatten(layered_circuit(n, 1, seed_for(3))))
+    a.apply_gates(flatten(layered_circuit(n, 1, workload_seed("layered_30q"))))
     b = a.clone()
     draws = [float(x) for x in np.random.default_rng(30).uniform(size=n)]
     a.synchronize()
@@ -607,7 +607,7 @@ def measure_section(q, torch, args) -> dict:
 
 
 def width_section(q, torch, args) -> dict:
-    """The plain form at scale (C2): a 28-qubit complex128 layered circuit (Haar on every qubit + a CNOT
+    """The plain form at scale: a 28-qubit complex128 layered circuit (Haar on every qubit + a CNOT
     matching per layer) with fusion off (one sweep per gate), cache-blocked stages, and dense fused
     blocks of width 2..5 (each block one sweep or one tensor-core stage). Per variant: ms, gates/s,
     sweeps, and the HBM GB/s those sweeps move (each gate's own bytes unfused, 2 * 2^n * 16 bytes per
@@ -616,7 +616,7 @@ def width_section(q, torch, args) -> dict:
     split-integer products on the BF16 tensor cores; every width pads its blocks to 5 qubits), and
     double-float (`df64`, narrower than FP64: 24 + 24 significand bits) for comparison. Layers: 40,
     except 10 for the FP64 blocks of 3..5 qubits, whose FP64 dense sweeps are slow."""
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
 
     n = 28
     lib = q._lib.load()
@@ -634,7 +634,7 @@ def width_section(q, torch, args) -> dict:
                 ("df64_unfused", "df64", 0, 5, 40), ("df64_blocks_w3", "df64", 2, 3, 40)]
     for name, ar, fuse, width, layers in variants:
         reg.set_arith(A[ar])
-        ops = flatten(layered_circuit(n, layers, seed_for(2)))
+        ops = flatten(layered_circuit(n, layers, workload_seed("layered_28q")))
         reg.apply_gates(ops[: 3 * (n + n // 2)], fuse=fuse, max_width=width)  # warm-up: 3 layers
         reg.synchronize()
         a = torch.cuda.Event(enable_timing=True)
@@ -662,10 +662,10 @@ def precision_section(q, torch, args) -> dict:
     (register passes, and 5-qubit dense blocks as 3xTF32 tensor-core GEMMs), with
     1 - F = 1 - |<x|fp64>|^2 / (<x|x><fp64|fp64>) accumulated in FP64 on the GPU after every 10
     layers, and the gates/s of each form."""
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
 
     n = args.qubits
-    layers = layered_circuit(n, 40, seed_for(3))
+    layers = layered_circuit(n, 40, workload_seed("layered_30q"))
     torch.cuda.synchronize()
     regs = {"fp64_plain": q.Register.from_int(n, 0),
             "c128_fx64": q.Register.from_int(n, 0),
@@ -717,9 +717,9 @@ def adjoint_section(q, torch, args) -> dict:
     """Gradient throughput on the 20-qubit, 10-layer ansatz (400 parameters, ZZ + X chain observable):
     FP64 (complex128, FP64 FMA arithmetic), complex128 with double-float arithmetic, and mixed (complex64
     state, FP64 accumulations), with the mixed run's 1 - F."""
-    from quaru_gb300.workloads import config4
+    from quaru_gb300.workloads import ansatz_problem
 
-    gates, params, terms = config4()
+    gates, params, terms = ansatz_problem()
     circuit, observable = q.ParamCircuit(gates), q.PauliSum(terms)  # converted once, as an optimiser loop would
     n = 20
     out = {"workload": "20-qubit hardware-efficient ansatz, 10 layers (RY, RZ on every qubit + CNOT ladder), "
@@ -756,9 +756,9 @@ def batch_section(q, args) -> dict:
     """256 ansatz circuits (10..22 qubits, 4..12 layers): one persistent graph replay per run (FP64,
     complex128 with double-float tiles, complex64) vs a loop of single-circuit adjoint calls (FP64)."""
     from quaru_gb300.batch import Batch
-    from quaru_gb300.workloads import config5
+    from quaru_gb300.workloads import ansatz_batch
 
-    circuits, params = config5()
+    circuits, params = ansatz_batch()
     params = np.array(params)
     ngrads = len(params)
     out = {"workload": "256 ansatz circuits, qubits ~ U{10..22}, layers ~ U{4..12}, random Z/ZZ/X observables",
@@ -813,7 +813,7 @@ def run_kernels(args) -> None:
     import quaru_gb300 as q
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
-    from quaru_gb300.workloads import config4, config5, flatten, layered_circuit
+    from quaru_gb300.workloads import ansatz_batch, ansatz_problem, flatten, layered_circuit
 
     n = args.qubits
     rng = np.random.default_rng(1)
@@ -855,12 +855,12 @@ def run_kernels(args) -> None:
         c.apply_gates(layers, fuse=2)
         c.measure(n - 1, 0.5)
         del r, c, p_reg
-    gates, params, terms = config4()
+    gates, params, terms = ansatz_problem()
     for prec in (q.QS_PREC_C128, q.QS_PREC_C64):  # FP64 and mixed (complex64) adjoint gradients
         reg = q.Register.from_int(20, 0, precision=prec)
         reg.set_arith(q.QS_ARITH_FMA)
         reg.adjoint_gradient(gates, params, terms)
-    circuits, bp = config5(count=16, qmin=10, qmax=18, lmin=2, lmax=4, seed=3)
+    circuits, bp = ansatz_batch(count=16, qmin=10, qmax=18, lmin=2, lmax=4, seed=3)
     for prec in (q.QS_PREC_C128, q.QS_PREC_C64):
         b = Batch(circuits, precision=prec, chunk_log2=11, ctas_per_sm=2)
         b.run(bp)
@@ -875,12 +875,12 @@ def run_case(args) -> None:
     integer products on the tensor cores); stages-c64: the same layers as register passes;
     measure-all: every qubit of a dense complex128 register measured in one sequence."""
     import quaru_gb300 as q
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
 
     n = args.qubits
     if args.case.startswith("dense-"):
         arith = ARITH_CODES(q)[args.case.split("-", 1)[1]]
-        layer = layered_circuit(n, 1, seed_for(3))[0]
+        layer = layered_circuit(n, 1, workload_seed("layered_30q"))[0]
         r = q.Register.from_int(n, 0)
         r.set_arith(q.QS_ARITH_DF64)
         r.apply_gates(layer)  # a dense state
@@ -889,7 +889,7 @@ def run_case(args) -> None:
             r.try_apply_fast(g)
     elif args.case in ("blocks-c64", "stages-c64"):
         r = q.Register.from_int(n, 0, precision=q.QS_PREC_C64)
-        ops = flatten(layered_circuit(n, 2, seed_for(3)))
+        ops = flatten(layered_circuit(n, 2, workload_seed("layered_30q")))
         if args.case == "blocks-c64":
             r.apply_gates(ops, fuse=2, max_width=5)
         else:
@@ -897,11 +897,11 @@ def run_case(args) -> None:
     elif args.case == "blocks-fx64":
         r = q.Register.from_int(n, 0)
         r.set_arith(q.QS_ARITH_FX64)
-        r.apply_gates(flatten(layered_circuit(n, 2, seed_for(3))), fuse=2, max_width=5)
+        r.apply_gates(flatten(layered_circuit(n, 2, workload_seed("layered_30q"))), fuse=2, max_width=5)
     elif args.case == "measure-all":
         r = q.Register.from_int(n, 0)
         r.set_arith(q.QS_ARITH_FMA)
-        r.apply_gates(flatten(layered_circuit(n, 1, seed_for(3))))
+        r.apply_gates(flatten(layered_circuit(n, 1, workload_seed("layered_30q"))))
         r.measure_sequence(list(range(n)), [0.5] * n)
     else:
         raise SystemExit(f"unknown case {args.case}")

@@ -1,4 +1,5 @@
-"""Seeded synthetic workloads (the gate sets and circuit families of the benchmark configurations).
+"""Seeded synthetic workloads: the 12-qubit parity circuit, the layered random-circuit family, and
+hardware-efficient ansatz circuits (single and batched) for the gradient benchmarks.
 
 All randomness comes from SplitMix64 (Steele, Lea, Flood: "Fast splittable
 pseudorandom number generators", OOPSLA 2014) so that the GPU runs, the CPU
@@ -67,16 +68,26 @@ class SplitMix64:
         return np.ascontiguousarray(np.stack([q0, q1], axis=1))
 
 
-def seed_for(config_id: int) -> int:
-    return BASE_SEED + config_id
+# Base seed of each named workload (BASE_SEED + a fixed offset per workload).
+WORKLOAD_SEEDS = {
+    "parity_12q": BASE_SEED + 1,    # the 12-qubit, 200-gate parity circuit
+    "layered_28q": BASE_SEED + 2,   # the layered family at 28 qubits (and its smaller test instances)
+    "layered_30q": BASE_SEED + 3,   # the layered family of the 30-qubit gate-sweep benchmark (and its host samples)
+    "ansatz_20q": BASE_SEED + 4,    # the 20-qubit, 400-parameter ansatz and its observable
+    "ansatz_batch": BASE_SEED + 5,  # the batch of 256 ansatz circuits
+}
 
 
-# ---------------------------------------------------------------- configuration 1
-GATE_SET_C1 = ("H", "X", "Y", "Z", "PHASE", "CNOT", "SWAP", "TOFFOLI", "HAAR")
+def workload_seed(name: str) -> int:
+    return WORKLOAD_SEEDS[name]
+
+
+# ---------------------------------------------------------------- the parity circuit
+PARITY_GATE_SET = ("H", "X", "Y", "Z", "PHASE", "CNOT", "SWAP", "TOFFOLI", "HAAR")
 
 
 def random_gate(rng: SplitMix64, n: int, kind: str | None = None) -> Operation:
-    kind = kind or GATE_SET_C1[rng.randint(len(GATE_SET_C1))]
+    kind = kind or PARITY_GATE_SET[rng.randint(len(PARITY_GATE_SET))]
     if kind == "H":
         return O.hadamard(rng.randint(n))
     if kind == "X":
@@ -108,15 +119,15 @@ class ParityCircuit:
     draws: list[float]
 
 
-def config1_circuit(n: int = 12, m: int = 200, seed: int | None = None) -> ParityCircuit:
-    """n-qubit |0..0>, m gates uniform over GATE_SET_C1, then one draw per qubit for measuring q0..q(n-1)."""
-    rng = SplitMix64(seed_for(1) if seed is None else seed)
+def parity_circuit(n: int = 12, m: int = 200, seed: int | None = None) -> ParityCircuit:
+    """n-qubit |0..0>, m gates uniform over PARITY_GATE_SET, then one draw per qubit for measuring q0..q(n-1)."""
+    rng = SplitMix64(workload_seed("parity_12q") if seed is None else seed)
     gates = [random_gate(rng, n) for _ in range(m)]
     draws = [rng.uniform() for _ in range(n)]
     return ParityCircuit(n, gates, draws)
 
 
-# ---------------------------------------------------------------- configurations 2 and 3
+# ---------------------------------------------------------------- the layered random-circuit family
 def layered_circuit(n: int, depth: int, seed: int) -> list[list[Operation]]:
     """Per layer: a Haar-random 1-qubit unitary on every qubit (0..n-1), then CNOTs on a
     random perfect matching (control, target) = (p[2i], p[2i+1]) of a shuffled qubit list."""
@@ -135,7 +146,7 @@ def flatten(layers: list[list[Operation]]) -> list[Operation]:
     return [g for layer in layers for g in layer]
 
 
-# ---------------------------------------------------------------- configuration 4 (and 5)
+# ---------------------------------------------------------------- hardware-efficient ansatz circuits
 def ansatz(n: int, layers: int):
     """Hardware-efficient ansatz: per layer RY(theta) then RZ(theta) on every qubit, then a CNOT
     ladder i -> i+1 for i = 0..n-2. Returns (ParamGate list, number of parameters)."""
@@ -162,19 +173,19 @@ def chain_hamiltonian(n: int, rng: SplitMix64):
     return terms
 
 
-def config4(n: int = 20, layers: int = 10, seed: int | None = None):
-    rng = SplitMix64(seed_for(4) if seed is None else seed)
+def ansatz_problem(n: int = 20, layers: int = 10, seed: int | None = None):
+    rng = SplitMix64(workload_seed("ansatz_20q") if seed is None else seed)
     gates, npar = ansatz(n, layers)
     params = [2.0 * math.pi * rng.uniform() for _ in range(npar)]
     return gates, params, chain_hamiltonian(n, rng)
 
 
-def config5(count: int = 256, qmin: int = 10, qmax: int = 22, lmin: int = 4, lmax: int = 12,
-            seed: int | None = None):
+def ansatz_batch(count: int = 256, qmin: int = 10, qmax: int = 22, lmin: int = 4, lmax: int = 12,
+                 seed: int | None = None):
     """Batch of ansatz circuits: qubits ~ U{qmin..qmax}, layers ~ U{lmin..lmax}, parameters ~ U[0, 2pi),
     random Z / ZZ / X observables with N(0, 1) coefficients. Returns (circuits, params) where each circuit
     is (n, gates, nparams, terms) and params is the concatenation."""
-    rng = SplitMix64(seed_for(5) if seed is None else seed)
+    rng = SplitMix64(workload_seed("ansatz_batch") if seed is None else seed)
     circuits, params = [], []
     for _ in range(count):
         n = qmin + rng.randint(qmax - qmin + 1)

@@ -12,8 +12,8 @@ from quaru_gb300.operation import Operation
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
-def load_config1():
-    doc = json.loads((GOLDEN / "config1.json").read_text())
+def load_parity_golden():
+    doc = json.loads((GOLDEN / "parity12.json").read_text())
     gates = []
     for g in doc["gates"]:
         k = len(g["targets"])
@@ -24,7 +24,7 @@ def load_config1():
 
 
 def golden_state() -> np.ndarray:
-    return np.fromfile(GOLDEN / "config1_state.bin", dtype="<f8").view(np.complex128)
+    return np.fromfile(GOLDEN / "parity12_state.bin", dtype="<f8").view(np.complex128)
 
 
 def sha(a: np.ndarray) -> str:

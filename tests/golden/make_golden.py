@@ -1,9 +1,9 @@
 """Generate the committed golden fixtures from the CPU oracle.
 
-config1.json: the seeded 12-qubit, 200-gate parity circuit (gates as hex
+parity12.json: the seeded 12-qubit, 200-gate parity circuit (gates as hex
 floats, so replaying it needs no libm), the 12 measurement draws, the SHA-256
 of the oracle's amplitudes after the gates and after measuring q0..q11, and
-the measured bitstring. config1_state.bin: the post-gate amplitudes
+the measured bitstring. parity12_state.bin: the post-gate amplitudes
 (interleaved little-endian float64).
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -21,7 +21,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 from oracle.oracle import OracleRegister  # noqa: E402
-from quaru_gb300.workloads import config1_circuit  # noqa: E402
+from quaru_gb300.workloads import parity_circuit  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 
@@ -33,7 +33,7 @@ def sha(a: np.ndarray) -> str:
 
 
 def main() -> None:
-    c = config1_circuit()
+    c = parity_circuit()
     reg = OracleRegister.from_int(c.n, 0)
     reg.apply_sequence([(g.matrix, g.targets) for g in c.gates])
     post_gates = reg.state.copy()
@@ -54,9 +54,9 @@ def main() -> None:
         "bitstring": bits,
         "measure_probs": probs,
     }
-    (HERE / "config1.json").write_text(json.dumps(doc, indent=1))
-    post_gates.astype(np.complex128).view(np.float64).astype("<f8").tofile(HERE / "config1_state.bin")
-    print("wrote", HERE / "config1.json", "bits", "".join(map(str, bits)))
+    (HERE / "parity12.json").write_text(json.dumps(doc, indent=1))
+    post_gates.astype(np.complex128).view(np.float64).astype("<f8").tofile(HERE / "parity12_state.bin")
+    print("wrote", HERE / "parity12.json", "bits", "".join(map(str, bits)))
 
 
 if __name__ == "__main__":

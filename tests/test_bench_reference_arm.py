@@ -34,4 +34,4 @@ def test_cpu_sweep_stops_at_the_limit():
     runs = d["cpu_sweep"]["runs"]
     assert runs[0]["qubits"] == 12 and all(r["completed"] for r in runs[:-1]) and not runs[-1]["completed"]
     assert d["cpu_sweep"]["largest_completed_qubits"] == (runs[-2]["qubits"] if len(runs) > 1 else None)
-    assert d["c1"]["gates"] == 200 and len(d["c1"]["bitstring"]) == 12
+    assert d["parity_12q"]["gates"] == 200 and len(d["parity_12q"]["bitstring"]) == 12

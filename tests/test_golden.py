@@ -1,14 +1,14 @@
-"""The committed config-1 golden fixture, replayed on the oracle (CPU) and on the GPU engine."""
+"""The committed golden fixture of the 12-qubit parity circuit, replayed on the oracle (CPU) and on the GPU engine."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from tests.fixtures import floored_rel_err, golden_state, load_config1, sha, value_equal
+from tests.fixtures import floored_rel_err, golden_state, load_parity_golden, sha, value_equal
 
 
 def test_oracle_reproduces_golden(oracle_mod):
-    doc, gates, draws = load_config1()
+    doc, gates, draws = load_parity_golden()
     reg = oracle_mod.OracleRegister.from_int(doc["n"], 0)
     reg.apply_sequence([(g.matrix, g.targets) for g in gates])
     assert sha(reg.state) == doc["sha256_after_gates"]
@@ -22,7 +22,7 @@ def test_oracle_reproduces_golden(oracle_mod):
 def test_gpu_matches_golden_bit_exact():
     import quaru_gb300 as q
 
-    doc, gates, draws = load_config1()
+    doc, gates, draws = load_parity_golden()
     reg = q.Register.from_int(doc["n"], 0)
     for g in gates:  # one try_apply_fast call per gate, the reference's path
         reg.try_apply_fast(g)
@@ -43,7 +43,7 @@ def test_gpu_matches_golden_bit_exact():
 def test_gpu_measure_sequence_matches_golden_bit_exact():
     import quaru_gb300 as q
 
-    doc, gates, draws = load_config1()
+    doc, gates, draws = load_parity_golden()
     reg = q.Register.from_int(doc["n"], 0)
     reg.apply_gates(gates)
     bits = reg.measure_sequence(list(range(doc["n"])), draws)
@@ -56,7 +56,7 @@ def test_gpu_measure_sequence_matches_golden_bit_exact():
 def test_gpu_circuit_call_matches_golden(fuse):
     import quaru_gb300 as q
 
-    doc, gates, _ = load_config1()
+    doc, gates, _ = load_parity_golden()
     reg = q.Register.from_int(doc["n"], 0)
     reg.apply_gates(gates, fuse=fuse)
     assert value_equal(reg.state, golden_state())
@@ -66,7 +66,7 @@ def test_gpu_circuit_call_matches_golden(fuse):
 def test_gpu_fma_and_c64_within_tolerance():
     import quaru_gb300 as q
 
-    doc, gates, _ = load_config1()
+    doc, gates, _ = load_parity_golden()
     ref = golden_state()
     reg = q.Register.from_int(doc["n"], 0)
     reg.set_arith(q.QS_ARITH_FMA)

@@ -171,9 +171,9 @@ def test_adjoint_tiled_mixed_gates(n, precision, arith):
 def test_param_circuit_and_pauli_sum_match_plain_lists():
     """ParamCircuit / PauliSum (records converted once) give the same energy and gradient as lists."""
     import quaru_gb300 as q
-    from quaru_gb300.workloads import config4
+    from quaru_gb300.workloads import ansatz_problem
 
-    gates, params, terms = config4(n=12, layers=3)
+    gates, params, terms = ansatz_problem(n=12, layers=3)
     for precision in (0, 1):
         reg = q.Register.from_int(12, 0, precision=precision)
         e1, g1 = reg.adjoint_gradient(gates, params, terms)
@@ -181,13 +181,13 @@ def test_param_circuit_and_pauli_sum_match_plain_lists():
         assert e1 == e2 and np.array_equal(g1, g2)
 
 
-def test_adjoint_config4_size_fp64_and_mixed():
+def test_adjoint_20_qubit_ansatz_fp64_and_mixed():
     """20 qubits, 10 layers, 400 parameters: spot-check 6 parameters by parameter shift and central
     differences; the complex64 (mixed) gradient agrees with FP64 to 1e-4 and its state has 1 - F <= 1e-6."""
     import quaru_gb300 as q
-    from quaru_gb300.workloads import config4
+    from quaru_gb300.workloads import ansatz_problem
 
-    gates, params, terms = config4()
+    gates, params, terms = ansatz_problem()
     params = np.array(params)
     n = 20
     reg = q.Register.from_int(n, 0)

@@ -40,9 +40,9 @@ def test_tuner_times_every_candidate_and_keeps_the_fastest(prec, arith):
 def test_autotuned_circuits_match_the_oracle(arith):
     import quaru_gb300 as q
     from oracle import oracle
-    from quaru_gb300.workloads import config1_circuit, flatten, layered_circuit
+    from quaru_gb300.workloads import flatten, layered_circuit, parity_circuit
 
-    for n, ops in ((12, config1_circuit().gates), (14, flatten(layered_circuit(14, 6, 77)))):
+    for n, ops in ((12, parity_circuit().gates), (14, flatten(layered_circuit(14, 6, 77)))):
         o = oracle.OracleRegister.from_int(n, 0)
         for op in ops:
             o.try_apply_fast(op.matrix, op.targets)
@@ -60,9 +60,9 @@ def test_autotuned_circuits_match_the_oracle(arith):
 def test_autotune_off_uses_the_fixed_rules():
     import quaru_gb300 as q
     from oracle import oracle
-    from quaru_gb300.workloads import config1_circuit
+    from quaru_gb300.workloads import parity_circuit
 
-    c = config1_circuit()
+    c = parity_circuit()
     o = oracle.OracleRegister.from_int(c.n, 0)
     for op in c.gates:
         o.try_apply_fast(op.matrix, op.targets)

@@ -27,9 +27,9 @@ def test_batch_matches_single_circuit_path(precision, arith, tol):
     """Circuits of 3..13 qubits (one tile up to 11 qubits, several above); items of one tile (cl = 8)
     and autotuned; arith = 2: complex128 stages in double-float tiles."""
     from quaru_gb300.batch import Batch
-    from quaru_gb300.workloads import config5
+    from quaru_gb300.workloads import ansatz_batch
 
-    circuits, params = config5(count=24, qmin=3, qmax=13, lmin=1, lmax=4, seed=99)
+    circuits, params = ansatz_batch(count=24, qmin=3, qmax=13, lmin=1, lmax=4, seed=99)
     params = np.array(params)
     for cl in (0, 8):
         b = Batch(circuits, precision=precision, chunk_log2=cl, ctas_per_sm=2 if cl else 0, arith=arith)
@@ -53,9 +53,9 @@ def test_batch_larger_circuits_fixed_gates(precision, arith, tol):
     from quaru_gb300 import ParamGate
     from quaru_gb300 import operation as O
     from quaru_gb300.batch import Batch
-    from quaru_gb300.workloads import config5
+    from quaru_gb300.workloads import ansatz_batch
 
-    circuits, params = config5(count=6, qmin=12, qmax=16, lmin=2, lmax=3, seed=7)
+    circuits, params = ansatz_batch(count=6, qmin=12, qmax=16, lmin=2, lmax=3, seed=7)
     mixed = []
     for i, (n, gates, npar, terms) in enumerate(circuits):
         g = list(gates)
@@ -117,14 +117,14 @@ def _energy(n, gates, params, terms, precision=0):
 
 
 def test_batch_at_the_benchmark_size():
-    """The benchmark's batch itself: 256 circuits of 10..22 qubits with 4..12 layers (config5's defaults).
+    """The benchmark's batch itself: 256 circuits of 10..22 qubits with 4..12 layers (the defaults of ansatz_batch).
     FP64 (autotuned chunking, as the benchmark runs it), complex128 double-float and complex64 batches
     against the loop of FP64 single-circuit gradients; central finite differences (h = 1e-6) on
     parameters of the three largest circuits within 1e-6."""
     from quaru_gb300.batch import Batch
-    from quaru_gb300.workloads import config5
+    from quaru_gb300.workloads import ansatz_batch
 
-    circuits, params = config5()
+    circuits, params = ansatz_batch()
     params = np.array(params)
     re, rg = per_circuit(circuits, params, 0)
     for precision, arith, tol, cl, ct in [(0, 1, 1e-10, 0, 0), (0, 2, 1e-10, 12, 2), (1, 1, 2e-4, 12, 2)]:

@@ -220,12 +220,12 @@ def test_fusion_widths_at_28_qubits_match_unfused_fp64():
     blocks, 10 layers for 4- and 5-qubit blocks, double-float arithmetic as timed) against one FP64
     FMA sweep per gate on the same gates, within the 1e-12 floored bound."""
     import quaru_gb300 as q
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
 
     n = 28
     refs = {}
     for layers in (40, 10):
-        ops = flatten(layered_circuit(n, layers, seed_for(2)))
+        ops = flatten(layered_circuit(n, layers, workload_seed("layered_28q")))
         r = q.Register.from_int(n, 0)
         r.set_arith(q.QS_ARITH_FMA)
         r.apply_gates(ops, fuse=0)

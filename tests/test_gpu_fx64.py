@@ -93,9 +93,9 @@ def _max_err(q, orc, n, ops, arith):
 
 
 def test_fx64_is_at_least_as_close_to_the_oracle_as_fp64_fma(q, orc):
-    from quaru_gb300.workloads import config1_circuit, flatten, layered_circuit
+    from quaru_gb300.workloads import flatten, layered_circuit, parity_circuit
 
-    cases = [(12, config1_circuit().gates), (16, flatten(layered_circuit(16, 40, 4242)))]
+    cases = [(12, parity_circuit().gates), (16, flatten(layered_circuit(16, 40, 4242)))]
     for n, ops in cases:
         fx_max, fx_sum = _max_err(q, orc, n, ops, FX64)
         fma_max, fma_sum = _max_err(q, orc, n, ops, FMA)

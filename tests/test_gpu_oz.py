@@ -158,11 +158,11 @@ def test_oz_blocks_28_qubits_match_unfused_fp64():
     """The benchmark's 28-qubit width configuration (10 layers of the layered family) as FP64-accurate
     5-qubit tensor-core blocks against one FP64 FMA sweep per gate, within the 1e-12 floored bound."""
     import quaru_gb300 as q
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
     from tests.test_gpu_fusion import _floored_err_chunked
 
     n = 28
-    ops = flatten(layered_circuit(n, 10, seed_for(2)))
+    ops = flatten(layered_circuit(n, 10, workload_seed("layered_28q")))
     r = q.Register.from_int(n, 0)
     r.set_arith(FMA)
     r.apply_gates(ops, fuse=0)

@@ -171,9 +171,9 @@ def test_large_dense_and_hadamard_transform(q, orc):
 
 
 def test_random_circuit_c64_within_tolerance(q, orc):
-    from quaru_gb300.workloads import config1_circuit
+    from quaru_gb300.workloads import parity_circuit
 
-    c = config1_circuit(n=10, m=300, seed=77)
+    c = parity_circuit(n=10, m=300, seed=77)
     o, g = run_pair(q, orc, c.n, c.gates, precision=1)
     assert floored_rel_err(g, o) <= 1e-4
 
@@ -273,9 +273,9 @@ def test_from_qubits_product_state_bit_exact(q, orc, n):
 
 
 def test_apply_circuit_matches_single_calls(q):
-    from quaru_gb300.workloads import config1_circuit
+    from quaru_gb300.workloads import parity_circuit
 
-    c = config1_circuit(n=11, m=250, seed=5)
+    c = parity_circuit(n=11, m=250, seed=5)
     a = q.Register.from_int(c.n, 0)
     for gte in c.gates:
         a.apply(gte)
@@ -312,9 +312,9 @@ def test_error_codes(q):
 
 @pytest.mark.parametrize("n", [1, 2, 7, 12])
 def test_df64_random_circuits_within_tolerance(q, orc, n):
-    from quaru_gb300.workloads import config1_circuit
+    from quaru_gb300.workloads import parity_circuit
 
-    c = config1_circuit(n=max(n, 3), m=400, seed=300 + n) if n >= 3 else None
+    c = parity_circuit(n=max(n, 3), m=400, seed=300 + n) if n >= 3 else None
     rng = np.random.default_rng(310 + n)
     if c is None:
         from quaru_gb300.operation import Operation
@@ -364,10 +364,10 @@ def test_df64_deep_layered_circuit(q, orc):
 def layered18(orc):
     """The benchmarks' layered family (Haar 1q on every qubit + CNOTs on a random matching) at its
     full 40-layer depth on 18 qubits (1080 gates, the 28-qubit configuration's seed), on the oracle."""
-    from quaru_gb300.workloads import flatten, layered_circuit, seed_for
+    from quaru_gb300.workloads import flatten, layered_circuit, workload_seed
 
     n = 18
-    ops = flatten(layered_circuit(n, 40, seed_for(2)))
+    ops = flatten(layered_circuit(n, 40, workload_seed("layered_28q")))
     o = orc.OracleRegister.from_int(n, 0)
     for op in ops:
         o.try_apply_fast(op.matrix, op.targets)

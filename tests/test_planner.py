@@ -52,10 +52,10 @@ def run_emulator(exe, n, T, L, ops, state, mode="exact", max_ops=None, widest=Fa
 def cases():
     from quaru_gb300 import operation as O
     from quaru_gb300.operation import Operation
-    from quaru_gb300.workloads import SplitMix64, config1_circuit, flatten, layered_circuit, random_gate
+    from quaru_gb300.workloads import SplitMix64, flatten, layered_circuit, parity_circuit, random_gate
 
-    c = config1_circuit()
-    yield "config1", c.n, c.gates
+    c = parity_circuit()
+    yield "parity12", c.n, c.gates
     yield "layered14", 14, flatten(layered_circuit(14, 6, 3))
     rng = np.random.default_rng(3)
     sm = SplitMix64(11)
